@@ -1,0 +1,127 @@
+/*
+ * orbkit_gb300.h -- C ABI of the GB300 grid-evaluation library (liborbkit_gb300.so).
+ *
+ * Grid evaluation of contracted Cartesian/spherical Gaussian atomic orbitals and
+ * their derivatives, the MO contraction C.AO and the occupation-weighted density
+ * and its derivatives, on one GPU (sm_103a).  Every pointer argument named d_* is a
+ * device pointer owned by the caller; host arrays are named h_*.  All compute
+ * entry points are stream-ordered (they enqueue work on `stream` and return
+ * without synchronising) and allocate no memory.  Every function returns an
+ * okg_status: 0 on success, a negative code otherwise; okg_last_error() gives
+ * a message for the calling thread.
+ *
+ * Which reference interface each entry point replaces is stated beside it
+ * (orbkit file:line).
+ */
+#ifndef ORBKIT_GB300_H
+#define ORBKIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    OKG_OK = 0,
+    OKG_ERR_ARG = -1,          /* bad argument, size or pointer */
+    OKG_ERR_L = -2,            /* angular momentum above 4, or components of mixed L in one shell */
+    OKG_ERR_DRV = -3,          /* derivative code outside 0..9 */
+    OKG_ERR_CUDA = -4,         /* CUDA runtime error (launch, copy) */
+    OKG_ERR_ALLOC = -5,        /* device or host allocation failed */
+    OKG_ERR_TIMEOUT = -6,      /* a bounded device-side wait expired */
+    OKG_ERR_UNSUPPORTED = -7,  /* shape outside what the selected kernel supports */
+    OKG_ERR_DEVICE = -8        /* no usable sm_103 device */
+} okg_status;
+
+typedef void* okg_stream; /* a cudaStream_t; NULL is the legacy default stream */
+
+/* Derivative codes, as orbkit's validate_drv (orbkit/tools.py:225-239):
+ * 0 none, 1 x, 2 y, 3 z, 4 xx, 5 yy, 6 zz, 7 xy, 8 xz, 9 yz. */
+
+/* A grid.  regular == 0: vector grid, point i is (x[i], y[i], z[i]).
+ * regular == 1: the Nx x Ny x Nz grid spanned by the three coordinate vectors,
+ * flattened with x slowest and z fastest (orbkit/cy_grid.pyx:14-30); `offset`
+ * is the flattened index of the first point evaluated, npts the number of points. */
+typedef struct {
+    const double* d_x;
+    const double* d_y;
+    const double* d_z;
+    int64_t npts;
+    int64_t offset;
+    int32_t nx, ny, nz;
+    int32_t regular;
+} okg_grid;
+
+typedef struct okg_basis okg_basis;
+
+/* Library status. */
+const char* okg_status_string(int status);
+const char* okg_last_error(void);
+int okg_version(void);
+
+/* Create a basis from orbkit's flattened AO description.
+ * Replaces the argument list that orbkit's AOClass getters (orbkit/orbitals.py:336-385)
+ * hand to cy_core.aocreator (orbkit/cy_core.pyx:51-78):
+ *   h_shell_atom  = ao_spec.get_assign_cont_to_atoms()   (nshell)
+ *   h_shell_ncart = ao_spec.get_nlxlylz_per_cont()       (nshell)
+ *   h_shell_nprim = ao_spec.get_nprim_per_cont()         (nshell)
+ *   h_lxlylz      = ao_spec.get_lxlylz()                 (ncart x 3)
+ *   is_normalized = ao_spec.get_normalized()             (orbkit/c_support.c:177-188)
+ *   h_renorm      = ao_spec[0]['N'] or NULL              (orbkit/core.py:98-100)
+ * Spherical output (orbkit/core.py:135-176): nsph > 0 and, per spherical row r,
+ * the components h_sph_cart[h_sph_ptr[r] .. h_sph_ptr[r+1]) (listed Cartesian rows)
+ * with coefficients h_sph_coef; rows of one shell must be contiguous.
+ * Allocates the device tables on the current device; geometry and primitive
+ * exponents/coefficients are set by okg_basis_set_params. */
+int okg_basis_create(int natom, int nshell, const int* h_shell_atom, const int* h_shell_ncart,
+                     const int* h_shell_nprim, const int* h_lxlylz, int is_normalized, const double* h_renorm,
+                     int nsph, const int* h_sph_ptr, const int* h_sph_cart, const double* h_sph_coef,
+                     okg_basis** out);
+int okg_basis_destroy(okg_basis* basis);
+/* Number of Cartesian AOs, output AOs (spherical or Cartesian), shells, primitives, atoms. */
+int okg_basis_info(const okg_basis* basis, int* ncart, int* nao, int* nshell, int* nprim, int* natom);
+
+/* Set nuclear positions (d_geo, natom x 3, bohr; orbkit's geo_spec) and primitive
+ * exponents/coefficients (d_prim, nprim x 2 [alpha, c]; ao_spec.get_prim_coeffs()).
+ * Computes the per-primitive weights c * (2/pi)^(3/4) 2^L alpha^((2L+3)/4)
+ * (orbkit/c_support.c:177-188) on `stream`.  Later calls on the same basis must be
+ * ordered after this one (same stream, or synchronised). */
+int okg_basis_set_params(okg_basis* basis, const double* d_geo, const double* d_prim, okg_stream stream);
+
+/* AOs and AO derivatives on a grid, FP64.
+ * Replaces cy_core.aocreator + c_lcreator (orbkit/cy_core.pyx:51-78,
+ * orbkit/c_grid-based.c:9-79) followed by the 'N' factor and cartesian2spherical
+ * (orbkit/core.py:89-102).  h_drv[0..ndrv) are derivative codes; output slot d is
+ * d_out[(d * nao + k) * ld + i] for output AO k and point i (AO-major, points
+ * contiguous, as ao_list[k, i]).  exact_mixed = 0 evaluates codes 7..9 with orbkit's
+ * own formula (orbkit/c_support.c:121-168), 1 with the exact mixed derivative. */
+int okg_eval_ao(const okg_basis* basis, const okg_grid* grid, int ndrv, const int* h_drv, int exact_mixed,
+                double* d_out, int64_t ld, okg_stream stream);
+
+/* MOs and MO derivatives on a grid, FP64, with the AOs kept on chip.
+ * Replaces ao_creator followed by cy_core.mocreator (orbkit/core.py:107-132,
+ * orbkit/cy_core.pyx:82-101) for every drv of slice_rho's calc_mo branch
+ * (orbkit/core.py:250-263).  d_coeff is C_eff (nmo x ncart, row-major): the MO
+ * coefficients in the Cartesian basis (for spherical bases C_sph . T).  Output
+ * slot d is d_out[(d * nmo + m) * ld + i]. */
+int okg_eval_mo(const okg_basis* basis, const okg_grid* grid, int nmo, const double* d_coeff, int ndrv,
+                const int* h_drv, int exact_mixed, double* d_out, int64_t ld, okg_stream stream);
+
+/* Density and density derivatives, FP64, fused AO -> MO -> reduction.
+ * Replaces the density part of slice_rho (orbkit/core.py:266-304; also
+ * rho_compute_no_slice, orbkit/core.py:808-838):
+ *   rho        = sum_m occ_m MO_m^2
+ *   drho[d]    = sum_m 2 occ_m dMO_m MO_m                     (codes 1..3)
+ *              + sum_m 2 occ_m d_aMO_m d_bMO_m                (codes 4..9, two-letter selectors)
+ * d_rho[i], d_drho[d * ld + i]; d_drho may be NULL when ndrv == 0.
+ * d_mo_norm (nmo, or NULL) receives += sum_i MO_m(i)^2 (atomic, order not fixed). */
+int okg_rho(const okg_basis* basis, const okg_grid* grid, int nmo, const double* d_coeff, const double* d_occ,
+            int ndrv, const int* h_drv, int exact_mixed, double* d_rho, double* d_drho, int64_t ld,
+            double* d_mo_norm, okg_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ORBKIT_GB300_H */

@@ -1,0 +1,84 @@
+"""Build liborbkit_gb300.so (CUDA, sm_103a) in-tree with nvcc.
+
+    python -m orbkit_gb300.build            # build if sources changed
+    python -m orbkit_gb300.build --force
+
+Each translation unit in orbkit_gb300/csrc/*.cu is compiled in parallel to an
+object under orbkit_gb300/_build/ and linked into orbkit_gb300/liborbkit_gb300.so
+(the CUDA runtime linked statically).  Only -gencode arch=compute_103a,code=sm_103a
+is emitted: the library targets GB300 only.
+"""
+import concurrent.futures
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+LIB = os.path.join(HERE, "liborbkit_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++20", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
+         "-Xptxas", "-warn-spills"]
+
+
+def nvcc():
+    p = shutil.which("nvcc")
+    if p:
+        return p
+    p = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(p):
+        return p
+    raise RuntimeError("nvcc not found")
+
+
+def _deps():
+    return sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + [os.path.join(INCLUDE, "orbkit_gb300.h")])
+
+
+def _compile(src, verbose=False, extra=()):
+    obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
+    newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(d) for d in _deps()])
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep and not extra:
+        return obj, ""
+    cmd = [nvcc()] + ARCH + FLAGS + list(extra) + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stdout + r.stderr))
+    return obj, r.stdout + r.stderr
+
+
+def build(force=False, verbose=False, extra=()):
+    """Compile every csrc/*.cu for sm_103a and link the shared library; returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    if force:
+        for o in glob.glob(os.path.join(BUILD, "*.o")):
+            os.remove(o)
+    with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose, extra), srcs))
+    objs = [o for o, _ in results]
+    if verbose:
+        for _, log in results:
+            if log:
+                print(log)
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        tmp = LIB + ".tmp%d" % os.getpid()
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs + ["-lcuda"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            # libcuda may be absent on a build-only machine; the runtime does not need it at link time
+            cmd = [c for c in cmd if c != "-lcuda"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    path = build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print(path)

@@ -1,0 +1,312 @@
+"""Drop-in replacement for the grid path of orbkit.core, running on the GPU.
+
+Same names, arguments, return shapes and errors as orbkit/core.py:
+  ao_creator            core.py:38-105
+  mo_creator            core.py:107-132
+  cartesian2spherical   core.py:135-176
+  rho_compute           core.py:314-605
+  rho_compute_no_slice  core.py:607-839
+  calc_mo_matrix        core.py:841-941
+Inputs are orbkit objects (QCinfo or dict with geo_spec / ao_spec / mo_spec) or
+this package's equivalents; the grid comes from the module ``core.grid``
+(orbkit_gb300.grid by default, orbkit.grid after ``orbkit_gb300.install(orbkit)``)
+or from explicit x, y, z.  Results are float64 numpy arrays in orbkit's layouts.
+
+Work runs on the current CUDA device through liborbkit_gb300.so; there is no
+CPU path.  ``numproc`` and ``slice_length`` are accepted for compatibility: the
+GPU evaluates the grid in device-sized slices of its own.  Mixed second
+derivatives (drv 'xy', 'xz', 'yz') use orbkit's formula (orbkit/c_support.c:121-168)
+unless ``exact_mixed=True`` is given.
+"""
+import numpy
+
+from . import _lib
+from . import grid as _default_grid
+from .basis import get_basis
+from .qcinfo import unpack
+from .tools import require, validate_drv
+
+grid = _default_grid
+
+# points per device slice (bounded so that slice outputs stay a few GB)
+MAX_SLICE_BYTES = 4 << 30
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise _lib.OkgError(-8, "no CUDA device visible")
+    return torch
+
+
+def _grid_arrays(x, y, z, is_vector, use_module=True):
+    """Resolve the grid like orbkit: explicit arrays or the grid module."""
+    if use_module and all(v is None for v in (x, y, z, is_vector)) and not grid.is_initialized:
+        grid.grid_init(is_vector=True)
+    if x is None:
+        x = grid.x
+    if y is None:
+        y = grid.y
+    if z is None:
+        z = grid.z
+    if is_vector is None:
+        is_vector = grid.is_vector
+    x, y, z = require(x, "f"), require(y, "f"), require(z, "f")
+    if is_vector:
+        if len(x) != len(y) or len(x) != len(z):
+            raise ValueError("Dimensions of x-, y-, and z- coordinate differ!")
+        return x, y, z, True, (len(x),)
+    return x, y, z, False, (len(x), len(y), len(z))
+
+
+class _DeviceGrid:
+    """Coordinates on the device, sliced into okg_grid descriptors."""
+
+    def __init__(self, x, y, z, is_vector, device):
+        torch = _torch()
+        self.regular = not is_vector
+        self.npts = len(x) if is_vector else len(x) * len(y) * len(z)
+        self.shape = (len(x), len(y), len(z))
+        self.host = (x, y, z)
+        self.dev = None
+        if self.regular:
+            self.dev = tuple(torch.from_numpy(numpy.ascontiguousarray(v)).to(device) for v in (x, y, z))
+        self.device = device
+
+    def slice(self, i, j):
+        """okg_grid for points [i, j) and the device tensors that keep it alive."""
+        torch = _torch()
+        g = _lib.OkgGrid()
+        if self.regular:
+            xs = self.dev
+            g.offset, g.npts = i, j - i
+            g.nx, g.ny, g.nz = self.shape
+            g.regular = 1
+        else:
+            xs = tuple(torch.from_numpy(numpy.ascontiguousarray(v[i:j])).to(self.device, non_blocking=False)
+                       for v in self.host)
+            g.offset, g.npts = 0, j - i
+            g.nx = g.ny = g.nz = 0
+            g.regular = 0
+        g.d_x, g.d_y, g.d_z = xs[0].data_ptr(), xs[1].data_ptr(), xs[2].data_ptr()
+        return g, xs
+
+
+def _slices(npts, bytes_per_point):
+    step = max(1, min(npts, MAX_SLICE_BYTES // max(1, bytes_per_point)))
+    return [(i, min(i + step, npts)) for i in range(0, npts, step)] or [(0, 0)]
+
+
+def _drv_list(drv):
+    if drv is None:
+        return None
+    if isinstance(drv, str):
+        try:
+            validate_drv(drv)
+            return [drv]
+        except ValueError:
+            return list(drv)
+    try:
+        return list(drv)
+    except TypeError:
+        return [drv]
+
+
+def _eval(qc_geo, ao_spec, mo_spec, x, y, z, is_vector, what, drv_codes, exact_mixed=False, occ=None):
+    """Evaluate on the GPU.  what: 'ao' -> (ndrv, nao, npts); 'mo' -> (ndrv, nmo, npts);
+    'rho' -> (rho (npts,), drho (ndrv, npts))."""
+    torch = _torch()
+    L = _lib.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    b = get_basis(qc_geo, ao_spec, dev)
+    g = _DeviceGrid(x, y, z, is_vector, dev)
+    npts = g.npts
+    nd = len(drv_codes)
+    codes = _lib.int_array(drv_codes)
+    em = 1 if exact_mixed else 0
+    st = _lib.stream_handle()
+    if what == "ao":
+        out = numpy.empty((nd, b.nao, npts))
+        for (i, j) in _slices(npts, 8 * nd * b.nao):
+            if j <= i:
+                continue
+            gd, keep = g.slice(i, j)
+            o = torch.empty((nd, b.nao, j - i), dtype=torch.float64, device=dev)
+            _lib.check(L.okg_eval_ao(b.handle, gd, nd, codes, em, _lib.ptr(o), j - i, st))
+            out[:, :, i:j] = o.cpu().numpy()
+        return out
+    C = b.c_eff(mo_spec.get_coeffs())
+    nmo = C.shape[0]
+    if what == "mo":
+        out = numpy.empty((nd, nmo, npts))
+        for (i, j) in _slices(npts, 8 * nd * nmo):
+            if j <= i:
+                continue
+            gd, keep = g.slice(i, j)
+            o = torch.empty((nd, nmo, j - i), dtype=torch.float64, device=dev)
+            _lib.check(L.okg_eval_mo(b.handle, gd, nmo, _lib.ptr(C), nd, codes, em, _lib.ptr(o), j - i, st))
+            out[:, :, i:j] = o.cpu().numpy()
+        return out
+    if occ is None:
+        occ = numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64)
+    occ_d = torch.as_tensor(numpy.asarray(occ, dtype=numpy.float64), device=dev).contiguous()
+    rho = numpy.empty(npts)
+    drho = numpy.empty((nd, npts))
+    for (i, j) in _slices(npts, 8 * (1 + nd)):
+        if j <= i:
+            continue
+        gd, keep = g.slice(i, j)
+        r = torch.empty(j - i, dtype=torch.float64, device=dev)
+        dr = torch.empty((max(nd, 1), j - i), dtype=torch.float64, device=dev)
+        _lib.check(L.okg_rho(b.handle, gd, nmo, _lib.ptr(C), _lib.ptr(occ_d), nd, codes, em, _lib.ptr(r),
+                             _lib.ptr(dr), j - i, None, st))
+        rho[i:j] = r.cpu().numpy()
+        if nd:
+            drho[:, i:j] = dr[:nd].cpu().numpy()
+    return rho, drho
+
+
+def ao_creator(geo_spec, ao_spec, drv=None, x=None, y=None, z=None, is_vector=None, exact_mixed=False):
+    """AOs or AO derivatives on the grid: (NAO,) + N float64 (orbkit/core.py:38-105)."""
+    x, y, z, vec, N = _grid_arrays(x, y, z, is_vector)
+    code = validate_drv(drv)
+    out = _eval(geo_spec, ao_spec, None, x, y, z, vec, "ao", [code], exact_mixed)[0]
+    return out.reshape((out.shape[0],) + N) if not vec else out
+
+
+def mo_creator(ao_list, mo_spec):
+    """MOs from given AO values, MO = C . AO (orbkit/core.py:107-132; cy_core.pyx:82-101).
+
+    The AO values are an input here, so this is a plain FP64 GEMM (cuBLAS through
+    torch) on the device; the fused paths never materialise AO values."""
+    torch = _torch()
+    ao_list = require(ao_list, "f")
+    shape = ao_list.shape
+    coeffs = require(mo_spec.get_coeffs(), "f")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    A = torch.from_numpy(ao_list.reshape(shape[0], -1)).to(dev)
+    C = torch.from_numpy(coeffs).to(dev)
+    return (C @ A).cpu().numpy().reshape((len(coeffs),) + shape[1:])
+
+
+def cartesian2spherical(ao_list, ao_spec):
+    """Cartesian -> real spherical AOs (orbkit/core.py:135-176), as a device GEMM with
+    the transform T of orbkit's cart2sph table."""
+    torch = _torch()
+    from .basis import spherical_csr
+    ptr, idx, coef = spherical_csr(ao_spec)
+    ncart = len(ao_spec.get_lxlylz())
+    T = numpy.zeros((len(ptr) - 1, ncart))
+    for r in range(len(ptr) - 1):
+        for t in range(ptr[r], ptr[r + 1]):
+            T[r, idx[t]] += coef[t]
+    ao_list = require(ao_list, "f")
+    shape = ao_list.shape
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = torch.from_numpy(T).to(dev) @ torch.from_numpy(ao_list.reshape(shape[0], -1)).to(dev)
+    return out.cpu().numpy().reshape((T.shape[0],) + shape[1:])
+
+
+def rho_compute(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, numproc=1, slice_length=1e4,
+                vector=None, save_hdf5=False, exact_mixed=False, **kwargs):
+    """Density, MOs, AOs or their derivatives on the grid module's grid (orbkit/core.py:314-605)."""
+    if calc_ao and calc_mo:
+        raise ValueError("Choose either calc_ao=True or calc_mo=True")
+    elif calc_ao:
+        calc_mo = True
+    if numproc <= 0:
+        return rho_compute_no_slice(qc, calc_ao=calc_ao, calc_mo=calc_mo, drv=drv, laplacian=laplacian,
+                                    exact_mixed=exact_mixed, **kwargs)
+    if save_hdf5:
+        raise NotImplementedError("save_hdf5 is not supported by the GPU path")
+    if laplacian:
+        drv = ["xx", "yy", "zz"]
+    drv = _drv_list(drv)
+    geo, ao_spec, mo_spec = unpack(qc)
+    if not grid.is_initialized:
+        grid.grid_init()
+    vec = grid.is_vector
+    x, y, z, vec, N = _grid_arrays(grid.x, grid.y, grid.z, vec, use_module=False)
+    codes = [0] if drv is None else [validate_drv(d) for d in drv]
+    if calc_mo:
+        what = "ao" if calc_ao else "mo"
+        out = _eval(geo, ao_spec, mo_spec, x, y, z, vec, what, codes, exact_mixed)
+        if drv is None:
+            out = out[0]
+            return out.reshape((out.shape[0],) + N)
+        return out.reshape(out.shape[:2] + N)
+    rcodes = [] if drv is None else codes
+    rho, drho = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed)
+    rho = rho.reshape(N)
+    if drv is None:
+        return rho
+    drho = drho.reshape((len(drv),) + N)
+    if laplacian:
+        return rho, drho, drho.sum(axis=0)
+    return rho, drho
+
+
+def rho_compute_no_slice(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, return_components=False,
+                         x=None, y=None, z=None, is_vector=None, exact_mixed=False, **kwargs):
+    """Unsliced variant with optional components (orbkit/core.py:607-839)."""
+    if calc_ao and calc_mo:
+        raise ValueError("calc_ao and calc_mo are mutually exclusive arguments."
+                         "Use calc_mo and return_components instead!")
+    x, y, z, vec, N = _grid_arrays(x, y, z, is_vector)
+    geo, ao_spec, mo_spec = unpack(qc)
+    if laplacian:
+        drv = ["xx", "yy", "zz"]
+    drv = _drv_list(drv)
+    conv = lambda a: a if vec else a.reshape(a.shape[:-1] + N)
+    if drv is not None:
+        codes = [validate_drv(d) for d in drv]
+        dao = conv(_eval(geo, ao_spec, mo_spec, x, y, z, vec, "ao", codes, exact_mixed))
+        if calc_ao:
+            return dao
+        dmo = conv(_eval(geo, ao_spec, mo_spec, x, y, z, vec, "mo", codes, exact_mixed))
+        if calc_mo:
+            return (dao, dmo) if return_components else dmo
+    ao_list = conv(_eval(geo, ao_spec, mo_spec, x, y, z, vec, "ao", [0])[0]) if (calc_ao or return_components) else None
+    if calc_ao:
+        return ao_list
+    mo_list = conv(_eval(geo, ao_spec, mo_spec, x, y, z, vec, "mo", [0])[0]) if (calc_mo or return_components) else None
+    if calc_mo:
+        return (ao_list, mo_list) if return_components else mo_list
+    rcodes = [] if drv is None else codes
+    rho, drho = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed)
+    rho = conv(rho)
+    if drv is None:
+        return (ao_list, mo_list, rho) if return_components else rho
+    drho = conv(drho)
+    delta = (drho, drho.sum(axis=0)) if laplacian else (drho,)
+    return ((ao_list, mo_list, rho, dao, dmo) + delta) if return_components else (rho,) + delta
+
+
+def calc_mo_matrix(qc_a, qc_b=None, drv=None, numproc=1, slice_length=1e4, save_hdf5=False, **kwargs):
+    """Products MO_a(r) * dMO_b(r) on the grid (orbkit/core.py:841-941)."""
+    if save_hdf5:
+        raise NotImplementedError("save_hdf5 is not supported by the GPU path")
+    ibra = [0]
+    if drv is None:
+        drv = [None]
+        iket = [0]
+    elif not isinstance(drv, list):
+        drv = [None, drv]
+        iket = [1]
+    else:
+        drv = [None] + drv
+        iket = list(range(1, len(drv)))
+    if qc_b is None or qc_a is qc_b:
+        mo_ket = rho_compute(qc_a, calc_mo=True, drv=drv, **kwargs)
+        mo_bra = mo_ket[ibra]
+        mo_ket = mo_ket[iket]
+    else:
+        mo_bra = rho_compute(qc_a, calc_mo=True, drv=[drv[i] for i in ibra], **kwargs)
+        mo_ket = rho_compute(qc_b, calc_mo=True, drv=[drv[i] for i in iket], **kwargs)
+    nmo_a = mo_bra.shape[1]
+    nmo_b = mo_ket.shape[1]
+    out = numpy.zeros((mo_ket.shape[0], nmo_a) + mo_ket.shape[1:])
+    for n in range(nmo_a):
+        for m in range(nmo_b):
+            out[:, n, m] = mo_bra[:, n] * mo_ket[:, m]
+    return out

@@ -1,0 +1,53 @@
+"""Shared test helpers: golden fixtures, parity metrics, library build."""
+import os
+import platform
+
+import numpy
+
+from orbkit_gb300.qcinfo import from_arrays
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# Parity bar of the FP64 GPU path against the oracle / the reference's outputs:
+# every element satisfies |gpu - ref| <= FP64_RTOL * |ref| + FP64_ATOL_REL * max|ref|
+# (max over the compared array).  The second term covers elements that are
+# themselves cancellation residues (near nodes and sign changes), whose
+# absolute error is set by the size of the terms that cancel, not by their
+# own value.
+FP64_RTOL = 1e-12
+FP64_ATOL_REL = 1e-13
+
+
+def load_golden(name):
+    d = dict(numpy.load(os.path.join(GOLDEN, name), allow_pickle=False))
+    return from_arrays(d), d
+
+
+def is_x86():
+    return platform.machine() in ("x86_64", "AMD64")
+
+
+def rel_errors(a, b):
+    """(max normwise error max|a-b|/max|b|, max elementwise error over |b| > 1e-6 max|b|)."""
+    a = numpy.asarray(a, dtype=numpy.float64)
+    b = numpy.asarray(b, dtype=numpy.float64)
+    scale = numpy.abs(b).max() if b.size else 0.0
+    if scale == 0.0:
+        return float(numpy.abs(a - b).max() if a.size else 0.0), 0.0
+    d = numpy.abs(a - b)
+    m = numpy.abs(b) > 1e-6 * scale
+    elem = float((d[m] / numpy.abs(b[m])).max()) if m.any() else 0.0
+    return float(d.max() / scale), elem
+
+
+def assert_fp64_close(a, b, what="", rtol=FP64_RTOL, atol_rel=FP64_ATOL_REL):
+    a = numpy.asarray(a, dtype=numpy.float64)
+    b = numpy.asarray(b, dtype=numpy.float64)
+    assert a.shape == b.shape, "%s: shape %s != %s" % (what, a.shape, b.shape)
+    scale = numpy.abs(b).max() if b.size else 0.0
+    bound = rtol * numpy.abs(b) + atol_rel * scale
+    bad = numpy.abs(a - b) > bound
+    if bad.any():
+        i = numpy.unravel_index(numpy.argmax(numpy.abs(a - b) - bound), a.shape)
+        raise AssertionError("%s: %d elements outside |d| <= %g|ref| + %g max|ref|; worst at %s: %r vs %r "
+                             "(errors %s)" % (what, bad.sum(), rtol, atol_rel, i, a[i], b[i], rel_errors(a, b)))

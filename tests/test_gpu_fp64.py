@@ -1,0 +1,182 @@
+"""FP64 GPU path against the reference's golden outputs and the CPU oracle.
+
+Parity bar: |gpu - ref| <= 1e-12 |ref| + 1e-13 max|ref| elementwise (helpers.FP64_*).
+"""
+import ctypes
+
+import numpy
+import pytest
+
+from helpers import assert_fp64_close, load_golden
+
+pytestmark = pytest.mark.gpu
+
+DRV_ALL = [None, "x", "y", "z", "xx", "yy", "zz", "xy", "xz", "yz"]
+
+
+@pytest.fixture(scope="module")
+def core():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from orbkit_gb300 import build
+    build.build()
+    from orbkit_gb300 import core as c
+    return c
+
+
+def _check_outputs(core, qc, d, x, y, z, is_vector, drv_rho, tag):
+    drv_ao = DRV_ALL[:d["ao"].shape[0]]
+    for k, dv in enumerate(drv_ao):
+        a = core.ao_creator(qc.geo_spec, qc.ao_spec, drv=dv, x=x, y=y, z=z, is_vector=is_vector)
+        assert_fp64_close(a, d["ao"][k], "%s ao drv=%s" % (tag, dv))
+    mo = core.rho_compute_no_slice(qc, calc_mo=True, drv=drv_ao, x=x, y=y, z=z, is_vector=is_vector)
+    assert_fp64_close(mo, d["mo"], tag + " mo")
+    r, dr = core.rho_compute_no_slice(qc, drv=drv_rho, x=x, y=y, z=z, is_vector=is_vector)
+    assert_fp64_close(r, d["rho"], tag + " rho")
+    assert_fp64_close(dr, d["delta_rho"], tag + " delta_rho")
+    lap = core.rho_compute_no_slice(qc, laplacian=True, x=x, y=y, z=z, is_vector=is_vector)[-1]
+    assert_fp64_close(lap, d["laplacian"], tag + " laplacian")
+
+
+def test_golden_small_cartesian(core):
+    qc, d = load_golden("small_cart.npz")
+    _check_outputs(core, qc, d, d["x"], d["y"], d["z"], False, ["x", "y", "z", "xx", "xy", "yz"], "small")
+
+
+def test_golden_spherical_fg_renorm(core):
+    qc, d = load_golden("sph_fg_N.npz")
+    x, y, z = d["points"]
+    _check_outputs(core, qc, d, x, y, z, True, ["x", "y", "z"], "sph")
+
+
+def test_golden_normalized(core):
+    qc, d = load_golden("normalized.npz")
+    _check_outputs(core, qc, d, d["x"], d["y"], d["z"], False, ["x", "y", "z"], "normalized")
+
+
+def test_golden_reference_h2o(core):
+    """The reference's own test (test/grid_based/rho_compute.py) through the module-global grid."""
+    from orbkit_gb300 import grid
+    qc, d = load_golden("h2o_molden.npz")
+    grid.set_grid(d["x"], d["y"], d["z"], is_vector=False)
+    drv = [None, "x", "y", "z", "xx", "xy", "xz", "yy", "yz", "zz"]
+    assert_fp64_close(core.rho_compute(qc, slice_length=0), d["zero"], "rho")
+    assert_fp64_close(core.rho_compute(qc, numproc=2), d["one"], "rho numproc")
+    assert_fp64_close(core.rho_compute(qc, laplacian=True, slice_length=0)[-1], d["two"], "laplacian")
+    assert_fp64_close(core.rho_compute(qc, laplacian=True, numproc=0)[-1], d["three"], "laplacian no_slice")
+    assert_fp64_close(core.rho_compute(qc, calc_mo=True, drv=drv, slice_length=0), d["four"], "drv MOs")
+    r, dr = core.rho_compute(qc, drv=["x", "y", "z", "xy"])
+    assert_fp64_close(r, d["rho_xyz"], "rho")
+    assert_fp64_close(dr, d["delta_rho_xyzxy"], "delta_rho")
+    # vector form of the same grid
+    grid.grid2vector()
+    r2 = core.rho_compute(qc)
+    assert_fp64_close(r2, d["zero"].reshape(-1), "rho vector grid")
+    grid.reset_grid()
+
+
+def test_small_full_grid_vs_oracle(core):
+    """The 3-atom workload on its full 80^3 grid: rho and grad rho."""
+    import okref
+    from orbkit_gb300 import synthetic
+    w = synthetic.small()
+    qc = w["qc"]
+    x, y, z = w["grid"]
+    r, dr = core.rho_compute_no_slice(qc, drv=["x", "y", "z"], x=x, y=y, z=z, is_vector=False)
+    pts = okref.grid2vector(x, y, z)
+    ro, dro = okref.rho_threads(qc, *pts, drv=["x", "y", "z"], slice_length=4096)
+    assert_fp64_close(r.reshape(-1), ro, "rho")
+    assert_fp64_close(dr.reshape(3, -1), dro, "grad rho")
+
+
+def test_mid_subgrid_vs_oracle(core):
+    """The 20-atom workload (180 AOs, 40 MOs): a 24x20x16 block of its 160^3 grid, and
+    a ragged run of flattened points through the regular-grid offset path."""
+    import okref
+    from orbkit_gb300 import synthetic
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    x, y, z = gx[60:84], gy[70:90], gz[50:66]
+    r, dr = core.rho_compute_no_slice(qc, drv=["x", "y", "z"], x=x, y=y, z=z, is_vector=False)
+    pts = okref.grid2vector(x, y, z)
+    ro, dro = okref.rho_threads(qc, *pts, drv=["x", "y", "z"], slice_length=512)
+    assert_fp64_close(r.reshape(-1), ro, "rho")
+    assert_fp64_close(dr.reshape(3, -1), dro, "grad rho")
+
+
+def test_edge_sizes(core):
+    """1, 63, 64, 65 and 1000 points, a point on a nucleus and far-field points."""
+    import okref
+    from orbkit_gb300 import synthetic
+    w = synthetic.small()
+    qc = w["qc"]
+    rng = numpy.random.default_rng(3)
+    for n in (1, 63, 64, 65, 1000):
+        p = rng.uniform(-6, 6, (3, n))
+        p[:, 0] = qc.geo_spec[1]
+        if n > 2:
+            p[:, 1] = [40.0, -35.0, 50.0]
+        r, dr = core.rho_compute_no_slice(qc, drv=["x", "y", "z", "xy"], x=p[0], y=p[1], z=p[2], is_vector=True)
+        ro, dro = okref.rho_threads(qc, *p, drv=["x", "y", "z", "xy"], slice_length=64, nthreads=2)
+        assert_fp64_close(r, ro, "rho n=%d" % n)
+        assert_fp64_close(dr, dro, "drho n=%d" % n)
+        a = core.ao_creator(qc.geo_spec, qc.ao_spec, drv="yz", x=p[0], y=p[1], z=p[2], is_vector=True)
+        assert_fp64_close(a, okref.ao_creator(qc.geo_spec, qc.ao_spec, drv="yz", x=p[0], y=p[1], z=p[2]), "ao yz")
+
+
+def test_many_mos_multiple_passes(core):
+    """More MOs than one pass of the fused kernel holds (40 per pass for rho+grad)."""
+    import okref
+    from orbkit_gb300 import synthetic
+    rng = numpy.random.default_rng(7)
+    geo = synthetic.random_geometry(rng, 6, 8.0)
+    el = ["C", "O", "H", "H", "N", "H"]
+    ao = synthetic.build_basis(rng, el)
+    mo = synthetic.build_mos(rng, geo, ao, 70)
+    qc = synthetic.make_qc(geo, el, ao, mo)
+    p = rng.uniform(-5, 5, (3, 777))
+    r, dr = core.rho_compute_no_slice(qc, drv=["x", "y", "z"], x=p[0], y=p[1], z=p[2], is_vector=True)
+    ro, dro = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=128, nthreads=2)
+    assert_fp64_close(r, ro, "rho")
+    assert_fp64_close(dr, dro, "drho")
+    m = core.rho_compute_no_slice(qc, calc_mo=True, drv=["x", "xx"], x=p[0], y=p[1], z=p[2], is_vector=True)
+    mref = okref.rho_compute_no_slice(qc, calc_mo=True, drv=["x", "xx"], x=p[0], y=p[1], z=p[2])
+    assert_fp64_close(m, mref, "mo")
+
+
+def test_exact_mixed_derivatives(core):
+    """exact_mixed=True gives the true d2/dxdy (checked by central differences of d/dx)."""
+    from orbkit_gb300 import synthetic
+    qc = synthetic.small()["qc"]
+    rng = numpy.random.default_rng(9)
+    p = rng.uniform(-2, 2, (3, 50))
+    h = 1e-5
+    dxy = core.ao_creator(qc.geo_spec, qc.ao_spec, drv="xy", x=p[0], y=p[1], z=p[2], is_vector=True,
+                          exact_mixed=True)
+    fp = core.ao_creator(qc.geo_spec, qc.ao_spec, drv="x", x=p[0], y=p[1] + h, z=p[2], is_vector=True)
+    fm = core.ao_creator(qc.geo_spec, qc.ao_spec, drv="x", x=p[0], y=p[1] - h, z=p[2], is_vector=True)
+    fd = (fp - fm) / (2 * h)
+    assert numpy.abs(dxy - fd).max() <= 1e-5 * numpy.abs(fd).max()
+
+
+def test_c_abi_errors(core):
+    """Bad derivative codes and leading dimensions are rejected with status codes."""
+    import torch
+    from orbkit_gb300 import _lib
+    from orbkit_gb300.basis import get_basis
+    from orbkit_gb300 import synthetic
+    qc = synthetic.small()["qc"]
+    L = _lib.load()
+    b = get_basis(qc.geo_spec, qc.ao_spec, torch.device("cuda"))
+    x = torch.zeros(10, dtype=torch.float64, device="cuda")
+    g = _lib.OkgGrid(x.data_ptr(), x.data_ptr(), x.data_ptr(), 10, 0, 0, 0, 0, 0)
+    out = torch.empty((1, b.nao, 10), dtype=torch.float64, device="cuda")
+    assert L.okg_eval_ao(b.handle, ctypes.byref(g), 1, _lib.int_array([12]), 0, _lib.ptr(out), 10, None) == -3
+    assert L.okg_eval_ao(b.handle, ctypes.byref(g), 1, _lib.int_array([1]), 0, _lib.ptr(out), 5, None) == -1
+    g0 = _lib.OkgGrid(x.data_ptr(), x.data_ptr(), x.data_ptr(), 0, 0, 0, 0, 0, 0)
+    assert L.okg_eval_ao(b.handle, ctypes.byref(g0), 1, _lib.int_array([1]), 0, _lib.ptr(out), 0, None) == 0
+    gr = _lib.OkgGrid(x.data_ptr(), x.data_ptr(), x.data_ptr(), 10, 995, 10, 10, 10, 1)
+    assert L.okg_eval_ao(b.handle, ctypes.byref(gr), 1, _lib.int_array([0]), 0, _lib.ptr(out), 10, None) == -1
+    torch.cuda.synchronize()

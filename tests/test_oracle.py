@@ -1,0 +1,149 @@
+"""The oracle pinned against the reference's golden vectors and (where the
+reference tree is present) against the reference extension itself.  CPU only."""
+import numpy
+import pytest
+
+import okref
+from helpers import is_x86, load_golden
+
+DRV_ALL = [None, "x", "y", "z", "xx", "yy", "zz", "xy", "xz", "yz"]
+
+
+def _same(a, b, what):
+    """Bit-identical on x86-64 (the fixtures were made there); 1e-13 elsewhere (other libm)."""
+    if is_x86():
+        numpy.testing.assert_array_equal(a, b, err_msg=what)
+    else:
+        numpy.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-13 * numpy.abs(b).max(), err_msg=what)
+
+
+def test_reference_golden_h2o():
+    """test/grid_based/rho_compute.py:13-43 of the reference: rho, Laplacian and the
+    10-drv MO grids of H2O (molden, Cartesian) on the adjust_to_geo(2, 1) grid."""
+    qc, d = load_golden("h2o_molden.npz")
+    x, y, z = d["x"], d["y"], d["z"]
+    drv = [None, "x", "y", "z", "xx", "xy", "xz", "yy", "yz", "zz"]
+    _same(okref.rho_compute(qc, slice_length=0, x=x, y=y, z=z, is_vector=False), d["zero"], "rho")
+    _same(okref.rho_compute(qc, slice_length=11, x=x, y=y, z=z, is_vector=False), d["one"], "rho sliced")
+    _same(okref.rho_compute(qc, laplacian=True, slice_length=0, x=x, y=y, z=z, is_vector=False)[-1], d["two"],
+          "laplacian")
+    _same(okref.rho_compute_no_slice(qc, laplacian=True, x=x, y=y, z=z, is_vector=False)[-1], d["three"],
+          "laplacian no_slice")
+    _same(okref.rho_compute(qc, calc_mo=True, drv=drv, slice_length=0, x=x, y=y, z=z, is_vector=False), d["four"],
+          "drv MOs")
+    r, dr = okref.rho_compute(qc, drv=["x", "y", "z", "xy"], slice_length=0, x=x, y=y, z=z, is_vector=False)
+    _same(r, d["rho_xyz"], "rho")
+    _same(dr, d["delta_rho_xyzxy"], "delta_rho x,y,z,xy")
+
+
+@pytest.mark.parametrize("name,drv_rho", [("small_cart.npz", ["x", "y", "z", "xx", "xy", "yz"]),
+                                          ("normalized.npz", ["x", "y", "z"])])
+def test_golden_regular(name, drv_rho):
+    qc, d = load_golden(name)
+    x, y, z = d["x"], d["y"], d["z"]
+    drv_ao = DRV_ALL[:d["ao"].shape[0]]
+    for k, dv in enumerate(drv_ao):
+        _same(okref.rho_compute(qc, calc_ao=True, drv=[dv], x=x, y=y, z=z, is_vector=False)[0], d["ao"][k],
+              "ao drv=%s" % dv)
+    _same(okref.rho_compute(qc, calc_mo=True, drv=drv_ao, x=x, y=y, z=z, is_vector=False), d["mo"], "mo")
+    r, dr = okref.rho_compute(qc, drv=drv_rho, x=x, y=y, z=z, is_vector=False)
+    _same(r, d["rho"], "rho")
+    _same(dr, d["delta_rho"], "delta_rho")
+    _same(okref.rho_compute(qc, laplacian=True, x=x, y=y, z=z, is_vector=False)[-1], d["laplacian"], "laplacian")
+
+
+def test_golden_spherical_fg_renorm():
+    """Spherical basis with f and g shells and a per-AO 'N' factor, vector grid through the nuclei."""
+    qc, d = load_golden("sph_fg_N.npz")
+    x, y, z = d["points"]
+    for k, dv in enumerate(DRV_ALL):
+        _same(okref.rho_compute(qc, calc_ao=True, drv=[dv], x=x, y=y, z=z)[0], d["ao"][k], "ao drv=%s" % dv)
+    _same(okref.rho_compute(qc, calc_mo=True, drv=DRV_ALL, x=x, y=y, z=z), d["mo"], "mo")
+    r, dr = okref.rho_compute(qc, drv=["x", "y", "z"], x=x, y=y, z=z)
+    _same(r, d["rho"], "rho")
+    _same(dr, d["delta_rho"], "delta_rho")
+    _same(okref.rho_compute(qc, laplacian=True, x=x, y=y, z=z)[-1], d["laplacian"], "laplacian")
+
+
+def test_threaded_driver_matches_sliced():
+    qc, d = load_golden("small_cart.npz")
+    pts = okref.grid2vector(d["x"], d["y"], d["z"])
+    r, dr = okref.rho_threads(qc, *pts, drv=["x", "y", "z", "xx", "xy", "yz"], slice_length=7, nthreads=3)
+    _same(r, d["rho"].reshape(-1), "threads rho")
+    _same(dr, d["delta_rho"].reshape(6, -1), "threads delta_rho")
+
+
+def test_mixed_derivative_formula_is_the_references():
+    """drv 7..9 reproduce orbkit's formula (c_support.c:121-168), not the exact
+    mixed derivative: for p_x, d2/dxdy differs from a finite difference of d/dx."""
+    a, X, Y, Z = 0.7, 0.3, -0.4, 0.2
+    ref = okref.lib().okref_get_ao_xyz(X, Y, Z, 1, 0, 0, a, 7)
+    assert ref == pytest.approx(4 * a * a * X * X * Y + 1.0, rel=1e-15)
+    exact = (1 - 2 * a * X * X) * (-2 * a * Y)
+    assert abs(ref - exact) > 0.1
+
+
+def _reference():
+    import refpkg
+    return refpkg.load()
+
+
+@pytest.fixture(scope="module")
+def ref():
+    ok = _reference()
+    if ok is None:
+        pytest.skip("reference tree not available")
+    return ok
+
+
+def test_oracle_vs_reference_extension(ref):
+    """Bit-identical AO / MO / density against the reference's compiled cy_core on
+    the seeded mid-size molecule (random points)."""
+    from orbkit_gb300 import synthetic
+    from refpkg import to_reference_qc as ref_qc
+    d = synthetic.mid()
+    q = ref_qc(ref, d["qc"])
+    rng = numpy.random.default_rng(5)
+    x, y, z = rng.uniform(-10, 10, (3, 300))
+    for dv in DRV_ALL:
+        a = ref.core.ao_creator(q.geo_spec, q.ao_spec, drv=dv, x=x, y=y, z=z, is_vector=True)
+        b = okref.ao_creator(d["qc"].geo_spec, d["qc"].ao_spec, drv=dv, x=x, y=y, z=z)
+        numpy.testing.assert_array_equal(a, b, err_msg="ao drv=%s" % dv)
+    R = ref.core.rho_compute_no_slice(q, drv=["x", "y", "z", "xy", "zz"], x=x, y=y, z=z, is_vector=True)
+    O = okref.rho_compute_no_slice(d["qc"], drv=["x", "y", "z", "xy", "zz"], x=x, y=y, z=z)
+    numpy.testing.assert_array_equal(R[0], O[0])
+    numpy.testing.assert_array_equal(R[1], O[1])
+    t = okref.rho_threads(d["qc"], x, y, z, drv=["x", "y", "z", "xy", "zz"], slice_length=64, nthreads=2)
+    numpy.testing.assert_array_equal(R[0], t[0])
+    numpy.testing.assert_array_equal(R[1], t[1])
+
+
+def test_tables_and_flattening_vs_reference(ref):
+    from orbkit import tools as rtools
+    from orbkit.orbitals import AOClass as RAO
+    from orbkit_gb300 import synthetic, tools
+    for l in range(5):
+        assert [tuple(c) for c in rtools.exp[l]] == [tuple(c) for c in tools.cartesian_order[l]]
+        for m in range(-l, l + 1):
+            a = rtools.get_cart2sph(l, m)
+            b = tools.get_cart2sph(l, m)
+            assert [tuple(c) for c in a[0]] == [tuple(c) for c in b[0]]
+            numpy.testing.assert_array_equal(numpy.array(a[1]) * a[2], numpy.array(b[1]) * b[2])
+    assert rtools.lquant == tools.lquant
+    d = synthetic.mid()
+    rao = RAO(seq=[dict(s) for s in d["qc"].ao_spec.data])
+    rao.update()
+    for g in ("get_lxlylz", "get_nlxlylz_per_cont", "get_prim_coeffs", "get_nprim_per_cont",
+              "get_assign_cont_to_atoms", "get_normalized", "get_assign_lxlylz_to_cont"):
+        numpy.testing.assert_array_equal(getattr(d["qc"].ao_spec, g)(), getattr(rao, g)(), err_msg=g)
+
+
+def test_overlap_vs_reference(ref):
+    from orbkit import analytical_integrals as ai
+    from orbkit_gb300 import overlap, synthetic
+    from refpkg import to_reference_qc as ref_qc
+    for d in (synthetic.small(), synthetic.mid()):
+        q = ref_qc(ref, d["qc"])
+        S_ref = ai.get_ao_overlap(q.geo_spec, q.geo_spec, q.ao_spec)
+        S = overlap.ao_overlap(d["qc"].geo_spec, d["qc"].ao_spec)
+        numpy.testing.assert_allclose(S, S_ref, atol=1e-13)
