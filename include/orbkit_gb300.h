@@ -121,6 +121,25 @@ int okg_rho(const okg_basis* basis, const okg_grid* grid, int nmo, const double*
             int ndrv, const int* h_drv, int exact_mixed, double* d_rho, double* d_drho, int64_t ld,
             double* d_mo_norm, okg_stream stream);
 
+/* ---------------------------------------------------------------- mixed path
+ * rho and grad rho with the C.AO contraction on the tensor cores (tcgen05, BF16
+ * operands split three ways, FP32 accumulation), exponent arguments and the final
+ * density accumulation in FP64.  Same quantities as okg_rho with codes {1,2,3}
+ * (orbkit/core.py:266-300), within the error stated by the tests.
+ * A plan holds the tensor-core operand form of the MO coefficients. */
+typedef struct okg_mixed_plan okg_mixed_plan;
+/* Allocates the plan's device buffer (split coefficients, occupations, status word). */
+int okg_mixed_plan_create(const okg_basis* basis, int nmo, okg_mixed_plan** out);
+int okg_mixed_plan_destroy(okg_mixed_plan* plan);
+/* Split C_eff (nmo x ncart, FP64, device) into the BF16 operand tiles; copy occ (nmo). */
+int okg_mixed_set_coeffs(okg_mixed_plan* plan, const double* d_coeff, const double* d_occ, okg_stream stream);
+/* d_rho[i]; d_grad[c * ld + i] for c = x, y, z when want_grad. */
+int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, double* d_rho, double* d_grad,
+                  int64_t ld, okg_stream stream);
+/* Synchronising check of the plan's device status word (bounded tensor-core waits):
+ * OKG_ERR_TIMEOUT if a wait expired since the last check (the word is then cleared). */
+int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,7 +40,8 @@ static int dfact(int n) { return n <= 0 ? 1 : n * dfact(n - 2); }
 // contractions are pre-normalised) and the split single-precision copies used by
 // the mixed path.
 __global__ void prim_weights_kernel(const double* __restrict__ prim_in, const int* __restrict__ prim_L, int nprim,
-                                    int is_normalized, double* __restrict__ prim_out, float* __restrict__ prim32)
+                                    int is_normalized, double* __restrict__ prim_out, float* __restrict__ prim32,
+                                    PrimMx* __restrict__ prim_mx)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nprim) return;
@@ -59,6 +60,11 @@ __global__ void prim_weights_kernel(const double* __restrict__ prim_in, const in
     prim32[4 * i + 1] = (float)(al - (double)ah);
     prim32[4 * i + 2] = wh;
     prim32[4 * i + 3] = (float)(w - (double)wh);
+    PrimMx m;
+    m.a2 = al;
+    m.w = wh;
+    m.wa = (float)(w * a);
+    prim_mx[i] = m;
 }
 
 __global__ void atoms_kernel(const double* __restrict__ geo, int natom, double* __restrict__ atoms)
@@ -227,6 +233,33 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
         chunks.push_back(make_int4(s0, nshell, k0, k));
     }
 
+    // mixed-path chunks: whole shells, canonical columns, at most OKG_MKC per chunk
+    std::vector<int4> mchunks;
+    std::vector<int> mcol_cart;
+    {
+        int s0 = 0, col = 0;
+        for (int s = 0; s <= nshell; ++s) {
+            const int nk = s < nshell ? ncanon(shells[s].L) : 0;
+            if (s == nshell || col + nk > OKG_MKC) {
+                mchunks.push_back(make_int4(s0, s, col, 0));
+                const size_t base = mcol_cart.size();
+                mcol_cart.resize(base + OKG_MKC, -1);
+                for (int t = s0; t < s; ++t)
+                    for (int q = 0; q < ncanon(shells[t].L); ++q) {
+                        const int r = comp_row[shells[t].comp0 + q];
+                        if (r >= 0) mcol_cart[base + shells[t].mcol + q] = shells[t].cart0 + r;
+                    }
+                s0 = s;
+                col = 0;
+            }
+            if (s < nshell) {
+                shells[s].mcol = col;
+                col += nk;
+            }
+        }
+    }
+    std::vector<float> comp_g32(comp_g.begin(), comp_g.end());
+
     okg_basis* b = (okg_basis*)calloc(1, sizeof(okg_basis));
     if (!b) return set_error(OKG_ERR_ALLOC, "okg_basis_create: host allocation");
     Layout lay;
@@ -241,6 +274,10 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     const size_t o_scid = lay.take(sizeof(int) * (sph_cidx.size() + 1));
     const size_t o_scoef = lay.take(sizeof(double) * (sph_coef.size() + 1));
     const size_t o_chunks = lay.take(sizeof(int4) * chunks.size());
+    const size_t o_pmx = lay.take(sizeof(PrimMx) * nprim);
+    const size_t o_cg32 = lay.take(sizeof(float) * comp_g32.size());
+    const size_t o_mch = lay.take(sizeof(int4) * mchunks.size());
+    const size_t o_mcc = lay.take(sizeof(int) * mcol_cart.size());
     const size_t bytes = lay.take(0);
     char* blk = nullptr;
     cudaError_t e = cudaMalloc((void**)&blk, bytes);
@@ -263,6 +300,12 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
         e = cudaMemcpy(blk + o_scoef, sph_coef.data(), sizeof(double) * sph_coef.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(blk + o_cg32, comp_g32.data(), sizeof(float) * comp_g32.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(blk + o_mch, mchunks.data(), sizeof(int4) * mchunks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(blk + o_mcc, mcol_cart.data(), sizeof(int) * mcol_cart.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(blk);
         free(b);
@@ -281,6 +324,11 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     d.sph_cidx = (const int*)(blk + o_scid);
     d.sph_coef = (const double*)(blk + o_scoef);
     d.chunks = (const int4*)(blk + o_chunks);
+    d.prim_mx = (const PrimMx*)(blk + o_pmx);
+    d.comp_g32 = (const float*)(blk + o_cg32);
+    d.mchunks = (const int4*)(blk + o_mch);
+    d.mcol_cart = (const int*)(blk + o_mcc);
+    d.nmchunk = (int)mchunks.size();
     d.natom = natom;
     d.nshell = nshell;
     d.nprim = nprim;
@@ -329,6 +377,7 @@ extern "C" int okg_basis_set_params(okg_basis* b, const double* d_geo, const dou
     cudaStream_t st = (cudaStream_t)stream;
     atoms_kernel<<<(b->natom + 127) / 128, 128, 0, st>>>(d_geo, b->natom, (double*)b->dev.atoms);
     prim_weights_kernel<<<(b->nprim + 127) / 128, 128, 0, st>>>(d_prim, b->prim_L, b->nprim, b->is_normalized,
-                                                                 (double*)b->dev.prim, (float*)b->dev.prim32);
+                                                                 (double*)b->dev.prim, (float*)b->dev.prim32,
+                                                                 (PrimMx*)b->dev.prim_mx);
     return cuda_status(cudaGetLastError(), "okg_basis_set_params");
 }

@@ -50,6 +50,16 @@ struct Shell {
     int out0;   // first output row (Cartesian: cart0, spherical: first spherical row)
     int nout;   // output rows (ncart or number of spherical functions)
     int sph0;   // first spherical row's index into sph_ptr (spherical bases)
+    int mcol;   // mixed path: first column of this shell inside its chunk (canonical order)
+    int pad;
+};
+
+// Per-primitive data of the mixed path: alpha*log2(e) in FP64 (the exponent
+// argument stays FP64) and the weights w, w*alpha in FP32.
+struct PrimMx {
+    double a2;
+    float w;
+    float wa;
 };
 
 struct BasisDev {
@@ -63,9 +73,17 @@ struct BasisDev {
     const int* sph_cidx;     // canonical component index within the shell
     const double* sph_coef;  // coefficient x global factor
     const int4* chunks;      // nchunk x {first shell, end shell, first Cartesian row, end row}
+    const PrimMx* prim_mx;   // nprim (mixed path)
+    const float* comp_g32;   // comp_g in FP32 (mixed path)
+    const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= 64 columns)
+    const int* mcol_cart;    // nmchunk x 64: listed Cartesian row feeding each column, or -1
     int natom, nshell, nprim, ncart, nsph, spherical;
-    int max_nprim, nchunk;
+    int max_nprim, nchunk, nmchunk;
 };
+
+// Mixed path: chunks of whole shells with at most OKG_MKC canonical columns
+// (one 128-byte swizzle atom of BF16 values).
+#define OKG_MKC 64
 
 // Shells are grouped into chunks of at most KC listed Cartesian rows; the fused
 // kernels stage one chunk of AO values in shared memory at a time.

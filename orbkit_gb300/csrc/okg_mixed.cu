@@ -1,0 +1,553 @@
+// Mixed-precision fused density kernel: AO generation on the CUDA cores, the
+// C.AO contraction on the 5th-generation tensor cores (tcgen05, BF16 operands,
+// FP32 accumulation in TMEM), the density reduction in FP64.
+//
+// Reference computation: orbkit/core.py:179-304 (slice_rho: AO -> MO ->
+// rho = sum occ MO^2, d rho = sum 2 occ dMO MO) with the AO kernel of
+// orbkit/c_grid-based.c:9-79.
+//
+// Precision scheme (all errors against the FP64 oracle are measured by the tests):
+//   * exponent argument u = alpha*log2(e) * r^2 in FP64 (r^2 from FP64 coordinates);
+//     u is split exactly into a float integer part and fraction with integer bit
+//     operations, 2^-f is a degree-7 Taylor polynomial of exp in FP32 (Horner/FMA),
+//     2^-k is applied to the float exponent field;
+//   * radial sums, polynomials and angular factors in FP32;
+//   * each AO value v (FP32) is split v = b0 + b1 + b2 into three BF16 numbers,
+//     each MO coefficient (FP64) likewise; six MMAs per (channel, K-step) form
+//     b0c0 + b0c1 + b1c0 + b0c2 + b1c1 + b2c0 (the omitted products are below
+//     2^-24 relative), accumulated in FP32 in tensor memory;
+//   * rho and grad rho accumulate the per-MO products in FP64.
+//
+// Tile: 128 grid points (the MMA's M), N = MO block padded to a multiple of 16
+// (<= 64 per pass), K = canonical Cartesian AO columns in chunks of 64 (one
+// 128-byte swizzle atom of BF16).  Per chunk the CTA writes 4 channels x 3 parts
+// of A (128 x 64 BF16, K-major, SWIZZLE_128B) into shared memory, copies the
+// matching pre-split, pre-swizzled B block, and one thread issues 96 MMAs.
+// Accumulators: 4 channels x N FP32 columns of TMEM.  Persistent CTAs, one per SM.
+#include <stdio.h>
+
+#include <cuda_bf16.h>
+
+#include "okg_internal.cuh"
+
+namespace okg {
+namespace mx {
+
+constexpr int M = 128;
+constexpr int KC = OKG_MKC;           // 64 BF16 = 128 bytes
+constexpr int NT = 256;               // 8 warps
+constexpr int A_TILE = M * 128;       // bytes of one 128 x 64 BF16 sub-tile
+constexpr int A_BYTES = 12 * A_TILE;  // 4 channels x 3 parts
+constexpr int NMAX = 64;              // MO columns per pass
+constexpr long long WAIT_LIMIT = 1ll << 24;
+
+struct Params {
+    BasisDev B;
+    Grid g;
+    const uint4* bpack;    // [npass][nmchunk][3][npad x 128 B], pre-swizzled
+    const double* occ;     // [npass * npad], zero padded
+    int npass, npad;
+    int want_grad;
+    double* rho;
+    double* grad;          // 3 x ld
+    long long ld;
+    int* status;           // device status word: 1 = timeout
+    long long ntiles;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// SMEM matrix descriptor: K-major, SWIZZLE_128B, SBO = 1024 B (8-row group stride).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+    d |= (uint64_t)1 << 46;                 // descriptor version
+    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, K-major A and B.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M_, int N_)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N_ >> 3) << 17) | ((uint32_t)(M_ >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false (and raises the status word) if the phase does not
+// complete within WAIT_LIMIT polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status)
+{
+    for (long long it = 0; it < WAIT_LIMIT; ++it)
+        if (mbar_try(bar, parity)) return true;
+    atomicExch(status, 1);
+    return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Exact conversion of a double to float by truncating the mantissa (integer ops
+// only; values below 2^-126 in magnitude become 0).
+__device__ __forceinline__ float dbl_to_flt_trunc(double d)
+{
+    const int hi = __double2hiint(d);
+    const unsigned lo = (unsigned)__double2loint(d);
+    const int e = (hi >> 20) & 0x7FF;
+    if (e <= 896) return 0.0f;
+    const unsigned bits = ((unsigned)hi & 0x80000000u) | ((unsigned)(e - 896) << 23) |
+                          (((unsigned)hi & 0xFFFFFu) << 3) | (lo >> 29);
+    return __uint_as_float(bits);
+}
+
+// e^(-u ln 2) = 2^-u for an FP64 argument u >= 0 (u = alpha log2(e) r^2).
+// u = uh + r exactly with uh the float truncation of u; k = rint(uh),
+// f = (uh - k) + r in FP32 (uh - k is exact), |f| <= 0.5 + 2^-23.  2^-f by the
+// degree-7 Taylor series of exp(y), y = -f ln 2 (|y| < 0.35, truncation error
+// < 6e-9 relative), scaled by 2^-k through the exponent field.
+__device__ __forceinline__ float exp2_neg(double u)
+{
+    if (__double2hiint(u) >= 0x40690000) return 0.0f;  // u >= 200: 2^-u underflows in float
+    const int hi = __double2hiint(u);
+    const unsigned lo = (unsigned)__double2loint(u);
+    const double uh_d = __hiloint2double(hi, (int)(lo & 0xE0000000u));
+    const double rem = u - uh_d;  // exact
+    const float uh = dbl_to_flt_trunc(uh_d);
+    const float rf = dbl_to_flt_trunc(rem);
+    const float k = rintf(uh);
+    const float f = (uh - k) + rf;
+    const float y = -f * 0.693147180559945309f;
+    float p = 1.0f / 5040.0f;
+    p = fmaf(p, y, 1.0f / 720.0f);
+    p = fmaf(p, y, 1.0f / 120.0f);
+    p = fmaf(p, y, 1.0f / 24.0f);
+    p = fmaf(p, y, 1.0f / 6.0f);
+    p = fmaf(p, y, 0.5f);
+    p = fmaf(p, y, 1.0f);
+    p = fmaf(p, y, 1.0f);
+    const int ki = (int)k;
+    const int ebits = (int)((__float_as_uint(p) >> 23) & 0xFF) - ki;
+    if (ebits <= 0) return 0.0f;
+    return __uint_as_float(__float_as_uint(p) - ((unsigned)ki << 23));
+}
+
+// Split an FP32 value into three BF16 values with v = b0 + b1 + b2 to 2^-24.
+__device__ __forceinline__ void split3(float v, __nv_bfloat16& b0, __nv_bfloat16& b1, __nv_bfloat16& b2)
+{
+    b0 = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(b0);
+    b1 = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(b1);
+    b2 = __float2bfloat16_rn(r2);
+}
+
+// byte offset of element (row m, column k) in a 128 x 64 BF16 K-major SW128 tile
+__device__ __forceinline__ uint32_t sw128_off(int m, int k)
+{
+    return (uint32_t)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 3) ^ (m & 7)) & 7) << 4) + ((k & 7) << 1));
+}
+
+__global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* A_s = smem;                            // 12 x 16 KB
+    unsigned char* B_s = smem + A_BYTES;                  // 3 x npad x 128 B
+    const int bbytes = 3 * P.npad * 128;
+    double* red = (double*)(B_s + 3 * NMAX * 128);        // 4 x 128 doubles
+    uint64_t* bar = (uint64_t*)(red + 4 * M);
+    uint32_t* tmem_slot = (uint32_t*)(bar + 1);
+    int* abort_flag = (int*)(tmem_slot + 1);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
+    const uint32_t bar_a = smem_u32(bar);
+    const int ncols = 4 * P.npad;
+    const uint32_t tm_cols = ncols <= 32 ? 32 : ncols <= 64 ? 64 : ncols <= 128 ? 128 : 256;
+
+    // zero A once: padding columns are never written and must hold finite values
+    for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)A_s)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        mbar_init(bar_a, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(tm_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    uint32_t phase = 0;
+    const uint32_t idesc = idesc_bf16(M, P.npad);
+    const int prow = tid & (M - 1);  // point row of this thread in the tile
+    const int half = tid >> 7;       // generation: shells alternate between the two halves
+    const BasisDev& B = P.B;
+
+    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+        const long long p = tile * M + prow;
+        const bool valid = p < P.g.npts;
+        double x, y, z;
+        grid_point(P.g, valid ? p : P.g.npts - 1, x, y, z);
+        double rho_acc = 0.0, gx_acc = 0.0, gy_acc = 0.0, gz_acc = 0.0;
+
+        for (int pass = 0; pass < P.npass; ++pass) {
+            for (int c = 0; c < B.nmchunk; ++c) {
+                if (c > 0) {  // previous chunk's MMAs must be done before A/B are overwritten
+                    if (!mbar_wait(bar_a, phase, P.status)) *abort_flag = 1;
+                    phase ^= 1;
+                }
+                // B block of this (pass, chunk)
+                const uint4* src = P.bpack + ((long long)pass * B.nmchunk + c) * (bbytes / 16);
+                for (int i = tid; i < bbytes / 16; i += NT) ((uint4*)B_s)[i] = src[i];
+                // A: AO values of this chunk's shells for this thread's point
+                const int4 ck = B.mchunks[c];
+                int last_atom = -1;
+                double X = 0, Y = 0, Z = 0, rr = 0;
+                float Xf = 0, Yf = 0, Zf = 0;
+                for (int s = ck.x + half; s < ck.y; s += 2) {
+                    const Shell sh = B.shells[s];
+                    if (sh.atom != last_atom) {
+                        X = x - B.atoms[4 * sh.atom];
+                        Y = y - B.atoms[4 * sh.atom + 1];
+                        Z = z - B.atoms[4 * sh.atom + 2];
+                        rr = X * X + Y * Y + Z * Z;
+                        Xf = (float)X;
+                        Yf = (float)Y;
+                        Zf = (float)Z;
+                        last_atom = sh.atom;
+                    }
+                    float R0 = 0.f, R1 = 0.f;
+                    for (int q = 0; q < sh.nprim; ++q) {
+                        const PrimMx pm = B.prim_mx[sh.prim0 + q];
+                        const float e = exp2_neg(pm.a2 * rr);
+                        R0 = fmaf(pm.w, e, R0);
+                        R1 = fmaf(pm.wa, e, R1);
+                    }
+                    const Radial<float> r{R0, R1, 0.f};
+                    shell_eval_L(sh.L, Xf, Yf, Zf, r, 0xFu, false, [&](int ch, int j, float v) {
+                        v *= B.comp_g32[sh.comp0 + j];
+                        __nv_bfloat16 b0, b1, b2;
+                        split3(v, b0, b1, b2);
+                        const uint32_t off = sw128_off(prow, sh.mcol + j);
+                        unsigned char* base = A_s + ch * 3 * A_TILE + off;
+                        *(__nv_bfloat16*)(base) = b0;
+                        *(__nv_bfloat16*)(base + A_TILE) = b1;
+                        *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
+                    });
+                }
+                fence_proxy_async();
+                __syncthreads();
+                if (tid == 0 && !*abort_flag) {
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(A_s), b0 = smem_u32(B_s);
+                    const int bpart = P.npad * 128;
+#pragma unroll 1
+                    for (int ch = 0; ch < 4; ++ch) {
+                        const uint32_t d = tmem + ch * P.npad;
+#pragma unroll
+                        for (int k = 0; k < KC / 16; ++k) {
+                            // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
+                            const int pa[6] = {0, 0, 1, 0, 1, 2};
+                            const int pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+                            for (int t = 0; t < 6; ++t) {
+                                const uint64_t ad = sdesc(a0 + (ch * 3 + pa[t]) * A_TILE + k * 32);
+                                const uint64_t bd = sdesc(b0 + pb[t] * bpart + k * 32);
+                                const uint32_t acc = (c > 0 || k > 0 || t > 0) ? 1u : 0u;
+                                mma_bf16(d, ad, bd, idesc, acc);
+                            }
+                        }
+                    }
+                    mma_commit(bar_a);
+                } else if (tid == 0) {
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_a) : "memory");
+                }
+            }
+            // accumulators of this pass complete
+            if (!mbar_wait(bar_a, phase, P.status)) *abort_flag = 1;
+            phase ^= 1;
+            tc_fence_after();
+            // epilogue: warp w reads TMEM lanes 32*(w%4).. (its 32 points), MO half w/4
+            {
+                const int q = warp & 3, h = warp >> 2;
+                const int nh = P.npad / 2;
+                const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
+                double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
+                for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
+                    float v0[8], v1[8], v2[8], v3[8];
+                    tmem_ld8(tl + 0 * P.npad + m0, v0);
+                    tmem_ld8(tl + 1 * P.npad + m0, v1);
+                    tmem_ld8(tl + 2 * P.npad + m0, v2);
+                    tmem_ld8(tl + 3 * P.npad + m0, v3);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const double o = __ldg(P.occ + pass * P.npad + m0 + i);
+                        racc = fma(o, (double)(v0[i] * v0[i]), racc);
+                        const double o2 = 2.0 * o;
+                        ga = fma(o2, (double)(v0[i] * v1[i]), ga);
+                        gb = fma(o2, (double)(v0[i] * v2[i]), gb);
+                        gc = fma(o2, (double)(v0[i] * v3[i]), gc);
+                    }
+                }
+                const int pt = 32 * q + lane;
+                if (h == 1) {
+                    red[pt] = racc;
+                    red[M + pt] = ga;
+                    red[2 * M + pt] = gb;
+                    red[3 * M + pt] = gc;
+                }
+                tc_fence_before();
+                __syncthreads();
+                if (h == 0) {
+                    // this thread owns point pt of the tile for the output
+                    racc += red[pt];
+                    ga += red[M + pt];
+                    gb += red[2 * M + pt];
+                    gc += red[3 * M + pt];
+                    // point pt belongs to thread pt (tid < 128 <=> h == 0 for warps 0..3)
+                    rho_acc += racc;
+                    gx_acc += ga;
+                    gy_acc += gb;
+                    gz_acc += gc;
+                }
+                __syncthreads();
+                tc_fence_after();
+            }
+        }
+        // threads 0..127 hold the totals of point tid (warp w<4, lane l -> point 32w + l == tid)
+        if (tid < M && valid && !*abort_flag) {
+            P.rho[p] = rho_acc;
+            if (P.want_grad) {
+                P.grad[p] = gx_acc;
+                P.grad[P.ld + p] = gy_acc;
+                P.grad[2 * P.ld + p] = gz_acc;
+            }
+        }
+        if (*abort_flag) break;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tm_cols));
+}
+
+// Split C_eff (nmo x ncart, FP64) into three BF16 parts in the B operand layout:
+// bpack[pass][chunk][part] is an npad x 64 K-major SWIZZLE_128B tile whose column
+// kk holds the coefficient of the listed Cartesian AO feeding mixed column kk.
+__global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, const int* __restrict__ mcol_cart,
+                              int nmchunk, int npass, int npad, __nv_bfloat16* __restrict__ bpack)
+{
+    const long long total = (long long)npass * nmchunk * npad * KC;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int kk = (int)(i % KC);
+        const int n = (int)((i / KC) % npad);
+        const int c = (int)((i / ((long long)KC * npad)) % nmchunk);
+        const int pass = (int)(i / ((long long)KC * npad * nmchunk));
+        const int mo = pass * npad + n;
+        const int cart = mcol_cart[c * KC + kk];
+        double v = (mo < nmo && cart >= 0) ? C[(long long)mo * ncart + cart] : 0.0;
+        const __nv_bfloat16 h0 = __double2bfloat16(v);
+        const double r1 = v - (double)__bfloat162float(h0);
+        const __nv_bfloat16 h1 = __double2bfloat16(r1);
+        const double r2 = r1 - (double)__bfloat162float(h1);
+        const __nv_bfloat16 h2 = __double2bfloat16(r2);
+        const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((kk >> 3) ^ (n & 7)) & 7) << 4) +
+                                        ((kk & 7) << 1));
+        unsigned char* blk = (unsigned char*)bpack + ((long long)pass * nmchunk + c) * (3ll * npad * 128);
+        *(__nv_bfloat16*)(blk + off) = h0;
+        *(__nv_bfloat16*)(blk + npad * 128 + off) = h1;
+        *(__nv_bfloat16*)(blk + 2 * npad * 128 + off) = h2;
+    }
+}
+
+__global__ void pack_occ_kernel(const double* __restrict__ occ, int nmo, int total, double* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < total) out[i] = i < nmo ? occ[i] : 0.0;
+}
+
+}  // namespace mx
+}  // namespace okg
+
+using namespace okg;
+
+struct okg_mixed_plan {
+    const okg_basis* basis;
+    int nmo, npad, npass;
+    void* block;       // bpack | occ | status
+    size_t bpack_bytes;
+    __nv_bfloat16* bpack;
+    double* occ;
+    int* status;
+    int sm_count;
+    size_t smem;
+};
+
+extern "C" int okg_mixed_plan_create(const okg_basis* b, int nmo, okg_mixed_plan** out)
+{
+    if (!out || !b || nmo <= 0) return set_error(OKG_ERR_ARG, "okg_mixed_plan_create: NULL basis/out or nmo <= 0");
+    *out = nullptr;
+    int dev = 0, major = 0, minor = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (major != 10 || minor != 3) return set_error(OKG_ERR_DEVICE, "okg_mixed_plan_create: needs an sm_103 GPU");
+    okg_mixed_plan* p = (okg_mixed_plan*)calloc(1, sizeof(okg_mixed_plan));
+    if (!p) return set_error(OKG_ERR_ALLOC, "okg_mixed_plan_create: host allocation");
+    p->basis = b;
+    p->nmo = nmo;
+    p->npass = (nmo + mx::NMAX - 1) / mx::NMAX;
+    const int per = (nmo + p->npass - 1) / p->npass;
+    p->npad = (per + 15) / 16 * 16;
+    p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * 128;
+    const size_t occ_off = (p->bpack_bytes + 255) & ~(size_t)255;
+    const size_t st_off = occ_off + (((size_t)p->npass * p->npad * 8 + 255) & ~(size_t)255);
+    cudaError_t e = cudaMalloc(&p->block, st_off + 256);
+    if (e != cudaSuccess) {
+        free(p);
+        return cuda_status(e, "okg_mixed_plan_create: cudaMalloc");
+    }
+    p->bpack = (__nv_bfloat16*)p->block;
+    p->occ = (double*)((char*)p->block + occ_off);
+    p->status = (int*)((char*)p->block + st_off);
+    cudaMemset(p->status, 0, sizeof(int));
+    p->sm_count = sms;
+    p->smem = 1024 + mx::A_BYTES + 3 * mx::NMAX * 128 + 4 * mx::M * 8 + 64;
+    e = cudaFuncSetAttribute(mx::rho_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+    if (e != cudaSuccess) {
+        cudaFree(p->block);
+        free(p);
+        return cuda_status(e, "okg_mixed_plan_create: shared memory attribute");
+    }
+    *out = p;
+    return OKG_OK;
+}
+
+extern "C" int okg_mixed_plan_destroy(okg_mixed_plan* p)
+{
+    if (!p) return OKG_OK;
+    cudaError_t e = cudaFree(p->block);
+    free(p);
+    return cuda_status(e, "okg_mixed_plan_destroy");
+}
+
+extern "C" int okg_mixed_set_coeffs(okg_mixed_plan* p, const double* d_coeff, const double* d_occ, okg_stream stream)
+{
+    if (!p || !d_coeff || !d_occ) return set_error(OKG_ERR_ARG, "okg_mixed_set_coeffs: NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    const BasisDev& B = p->basis->dev;
+    mx::pack_b_kernel<<<p->sm_count * 4, 256, 0, st>>>(d_coeff, p->nmo, B.ncart, B.mcol_cart, B.nmchunk, p->npass,
+                                                       p->npad, p->bpack);
+    const int total = p->npass * p->npad;
+    mx::pack_occ_kernel<<<(total + 127) / 128, 128, 0, st>>>(d_occ, p->nmo, total, p->occ);
+    return cuda_status(cudaGetLastError(), "okg_mixed_set_coeffs");
+}
+
+extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_grad, double* d_rho, double* d_grad,
+                             int64_t ld, okg_stream stream)
+{
+    if (!p || !gr || !d_rho || (want_grad && !d_grad)) return set_error(OKG_ERR_ARG, "okg_rho_mixed: NULL argument");
+    Grid g;
+    g.x = gr->d_x;
+    g.y = gr->d_y;
+    g.z = gr->d_z;
+    g.npts = gr->npts;
+    g.offset = gr->offset;
+    g.nx = gr->nx;
+    g.ny = gr->ny;
+    g.nz = gr->nz;
+    g.regular = gr->regular;
+    if (g.npts < 0 || !g.x || !g.y || !g.z) return set_error(OKG_ERR_ARG, "okg_rho_mixed: bad grid");
+    if (g.regular && (g.nx <= 0 || g.ny <= 0 || g.nz <= 0 || g.offset < 0 ||
+                      g.offset + g.npts > (long long)g.nx * g.ny * g.nz))
+        return set_error(OKG_ERR_ARG, "okg_rho_mixed: regular grid range outside Nx*Ny*Nz");
+    if (g.npts == 0) return OKG_OK;
+    if (ld < g.npts) return set_error(OKG_ERR_ARG, "okg_rho_mixed: ld < npts");
+    mx::Params P;
+    P.B = p->basis->dev;
+    P.g = g;
+    P.bpack = (const uint4*)p->bpack;
+    P.occ = p->occ;
+    P.npass = p->npass;
+    P.npad = p->npad;
+    P.want_grad = want_grad;
+    P.rho = d_rho;
+    P.grad = d_grad;
+    P.ld = ld;
+    P.status = p->status;
+    P.ntiles = (g.npts + mx::M - 1) / mx::M;
+    const long long grid = P.ntiles < p->sm_count ? P.ntiles : p->sm_count;
+    mx::rho_mixed_kernel<<<(unsigned)grid, mx::NT, p->smem, (cudaStream_t)stream>>>(P);
+    return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
+}
+
+extern "C" int okg_mixed_status(okg_mixed_plan* p, int* device_status)
+{
+    if (!p || !device_status) return set_error(OKG_ERR_ARG, "okg_mixed_status: NULL argument");
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, p->status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e, "okg_mixed_status");
+    *device_status = v;
+    if (v) {
+        cudaMemset(p->status, 0, sizeof(int));
+        return set_error(OKG_ERR_TIMEOUT, "okg_rho_mixed: a tensor-core wait timed out");
+    }
+    return OKG_OK;
+}

@@ -1,0 +1,189 @@
+"""Mixed-precision rho and grad rho on the tensor cores.
+
+The C.AO contraction runs in BF16 on tcgen05 tensor cores with every operand
+split into three BF16 parts (six MMAs per product, FP32 accumulation); the
+exponent arguments and the final density accumulation stay FP64.  Points
+within ``cusp_radius`` bohr of a nucleus are recomputed with the FP64 path
+(the cusp region stays FP64).
+
+Error bar (measured by tests/test_gpu_mixed.py against the FP64 path, which itself
+matches the oracle to 1e-12): max relative rho error <= MIXED_RHO_RTOL over
+points with rho > MIXED_RHO_FLOOR.
+"""
+import ctypes
+
+import numpy
+
+from . import _lib
+from .basis import get_basis
+from .qcinfo import unpack
+
+MIXED_RHO_RTOL = 1e-6
+MIXED_RHO_FLOOR = 1e-10
+CUSP_RADIUS = 0.3
+
+_SIGS = {
+    "okg_mixed_plan_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "okg_mixed_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "okg_mixed_set_coeffs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "okg_rho_mixed": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_lib.OkgGrid), ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "okg_mixed_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+}
+
+
+def _L():
+    L = _lib.load()
+    for n, (r, a) in _SIGS.items():
+        f = getattr(L, n)
+        f.restype = r
+        f.argtypes = a
+    return L
+
+
+class MixedPlan:
+    """Tensor-core operand form of a set of MO coefficients for one DeviceBasis."""
+
+    def __init__(self, basis, coeffs, occ, stream=None):
+        import torch
+        self.basis = basis
+        self._L = _L()
+        C = basis.c_eff(coeffs)
+        self.nmo = C.shape[0]
+        self.occ = torch.as_tensor(numpy.asarray(occ, dtype=numpy.float64), device=basis.device).contiguous()
+        h = ctypes.c_void_p()
+        _lib.check(self._L.okg_mixed_plan_create(basis.handle, self.nmo, ctypes.byref(h)))
+        self._h = h
+        self.C = C
+        _lib.check(self._L.okg_mixed_set_coeffs(h, _lib.ptr(C), _lib.ptr(self.occ), _lib.stream_handle(stream)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def rho(self, grid_desc, rho, grad, ld, stream=None):
+        """Launch on an okg_grid; rho (npts) and grad (3, ld) are device tensors."""
+        _lib.check(self._L.okg_rho_mixed(self._h, grid_desc, 1 if grad is not None else 0, _lib.ptr(rho),
+                                         _lib.ptr(grad), ld, _lib.stream_handle(stream)))
+
+    def check(self):
+        st = ctypes.c_int(0)
+        _lib.check(self._L.okg_mixed_status(self._h, ctypes.byref(st)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._L.okg_mixed_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+def cusp_points_regular(geo, x, y, z, radius):
+    """Flattened indices of regular-grid points within `radius` of any nucleus."""
+    out = []
+    nyz = len(y) * len(z)
+    for A in numpy.asarray(geo, dtype=numpy.float64).reshape(-1, 3):
+        ix = numpy.nonzero(numpy.abs(x - A[0]) <= radius)[0]
+        iy = numpy.nonzero(numpy.abs(y - A[1]) <= radius)[0]
+        iz = numpy.nonzero(numpy.abs(z - A[2]) <= radius)[0]
+        if not (len(ix) and len(iy) and len(iz)):
+            continue
+        I, J, K = numpy.meshgrid(ix, iy, iz, indexing="ij")
+        d2 = (x[I] - A[0]) ** 2 + (y[J] - A[1]) ** 2 + (z[K] - A[2]) ** 2
+        m = d2 <= radius * radius
+        out.append((I[m] * nyz + J[m] * len(z) + K[m]).astype(numpy.int64))
+    if not out:
+        return numpy.zeros(0, dtype=numpy.int64)
+    return numpy.unique(numpy.concatenate(out))
+
+
+def rho_grad(qc, x, y, z, is_vector, cusp_radius=CUSP_RADIUS, return_device=False):
+    """rho and grad rho (3, npts) on the GPU mixed path, with the cusp region in FP64."""
+    import torch
+    from .core import _DeviceGrid
+    geo, ao_spec, mo_spec = unpack(qc)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    b = get_basis(geo, ao_spec, dev)
+    occ = numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64)
+    plan = MixedPlan(b, mo_spec.get_coeffs(), occ)
+    g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
+                    numpy.asarray(z, dtype=numpy.float64), is_vector, dev)
+    n = g.npts
+    rho = torch.empty(n, dtype=torch.float64, device=dev)
+    grad = torch.empty((3, n), dtype=torch.float64, device=dev)
+    gd, keep = g.slice(0, n)
+    plan.rho(gd, rho, grad, n)
+    if cusp_radius and cusp_radius > 0:
+        fix_cusp(plan, geo, g, rho, grad, cusp_radius)
+    plan.check()
+    if return_device:
+        return rho, grad
+    return rho.cpu().numpy(), grad.cpu().numpy()
+
+
+def fix_cusp(plan, geo, g, rho, grad, radius):
+    """Recompute the points within `radius` of a nucleus with the FP64 kernel."""
+    import torch
+    L = _lib.load()
+    dev = rho.device
+    if g.regular:
+        idx = cusp_points_regular(geo, *g.host, radius)
+        if len(idx) == 0:
+            return
+        gx, gy, gz = g.host
+        nyz = len(gy) * len(gz)
+        px = gx[idx // nyz]
+        py = gy[(idx // len(gz)) % len(gy)]
+        pz = gz[idx % len(gz)]
+        pts = torch.from_numpy(numpy.stack([px, py, pz])).to(dev)
+        it = torch.from_numpy(idx).to(dev)
+    else:
+        pts_all = torch.stack([torch.from_numpy(numpy.ascontiguousarray(v)).to(dev) for v in g.host])
+        G = torch.as_tensor(numpy.asarray(geo, dtype=numpy.float64), device=dev)
+        near = torch.zeros(pts_all.shape[1], dtype=torch.bool, device=dev)
+        for a in range(G.shape[0]):
+            near |= ((pts_all - G[a][:, None]) ** 2).sum(0) <= radius * radius
+        it = torch.nonzero(near).flatten()
+        if it.numel() == 0:
+            return
+        pts = pts_all[:, it].contiguous()
+    m = pts.shape[1]
+    gd = _lib.OkgGrid(pts[0].data_ptr(), pts[1].data_ptr(), pts[2].data_ptr(), m, 0, 0, 0, 0, 0)
+    r = torch.empty(m, dtype=torch.float64, device=dev)
+    dr = torch.empty((3, m), dtype=torch.float64, device=dev)
+    b = plan.basis
+    _lib.check(L.okg_rho(b.handle, gd, plan.nmo, _lib.ptr(plan.C), _lib.ptr(plan.occ), 3, _lib.int_array([1, 2, 3]),
+                         1, _lib.ptr(r), _lib.ptr(dr), m, None, _lib.stream_handle()))
+    rho.index_copy_(0, it, r)
+    grad.index_copy_(1, it, dr)
+
+
+def error_report(rho, grad, rho_ref, grad_ref, floor=MIXED_RHO_FLOOR):
+    """Max relative rho error over rho_ref > floor, max abs rho error, and the grad error
+    normalised by |grad_ref| + floor."""
+    rho = numpy.asarray(rho).reshape(-1)
+    rho_ref = numpy.asarray(rho_ref).reshape(-1)
+    m = rho_ref > floor
+    rel = numpy.abs(rho - rho_ref)[m] / rho_ref[m]
+    gr = numpy.asarray(grad).reshape(3, -1)
+    gref = numpy.asarray(grad_ref).reshape(3, -1)
+    gn = numpy.linalg.norm(gref, axis=0)
+    gerr = numpy.linalg.norm(gr - gref, axis=0) / (gn + floor)
+    return {
+        "rho_max_rel": float(rel.max()) if rel.size else 0.0,
+        "rho_p999_rel": float(numpy.percentile(rel, 99.9)) if rel.size else 0.0,
+        "rho_max_abs": float(numpy.abs(rho - rho_ref).max()),
+        "grad_max_rel": float(gerr.max()),
+        "floor": floor,
+        "points_above_floor": int(m.sum()),
+    }
+
+
+def smoke_check(qc, x, y, z, rho_ref, grad_ref):
+    r, g = rho_grad(qc, x, y, z, False)
+    rep = error_report(r, g, rho_ref, grad_ref)
+    assert rep["rho_max_rel"] <= MIXED_RHO_RTOL, rep
+    print("smoke mixed: rho max rel err %.2e (rho > %g), grad max rel err %.2e" % (
+        rep["rho_max_rel"], rep["floor"], rep["grad_max_rel"]))

@@ -45,8 +45,9 @@ def assert_fp64_close(a, b, what="", rtol=FP64_RTOL, atol_rel=FP64_ATOL_REL):
     b = numpy.asarray(b, dtype=numpy.float64)
     assert a.shape == b.shape, "%s: shape %s != %s" % (what, a.shape, b.shape)
     scale = numpy.abs(b).max() if b.size else 0.0
+    assert numpy.isfinite(b).all(), "%s: reference holds non-finite values" % what
     bound = rtol * numpy.abs(b) + atol_rel * scale
-    bad = numpy.abs(a - b) > bound
+    bad = ~(numpy.abs(a - b) <= bound)  # NaN in a counts as a mismatch
     if bad.any():
         i = numpy.unravel_index(numpy.argmax(numpy.abs(a - b) - bound), a.shape)
         raise AssertionError("%s: %d elements outside |d| <= %g|ref| + %g max|ref|; worst at %s: %r vs %r "

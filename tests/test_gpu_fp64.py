@@ -131,9 +131,9 @@ def test_many_mos_multiple_passes(core):
     import okref
     from orbkit_gb300 import synthetic
     rng = numpy.random.default_rng(7)
-    geo = synthetic.random_geometry(rng, 6, 8.0)
-    el = ["C", "O", "H", "H", "N", "H"]
-    ao = synthetic.build_basis(rng, el)
+    geo = synthetic.random_geometry(rng, 8, 9.0)
+    el = ["C", "O", "C", "H", "N", "H", "C", "H"]
+    ao = synthetic.build_basis(rng, el)  # 5 heavy x 15 + 3 H x 5 = 90 AOs
     mo = synthetic.build_mos(rng, geo, ao, 70)
     qc = synthetic.make_qc(geo, el, ao, mo)
     p = rng.uniform(-5, 5, (3, 777))
