@@ -15,7 +15,12 @@
 //   * each AO value v (FP32) is split v = b0 + b1 + b2 into three BF16 numbers,
 //     each MO coefficient (FP64) likewise; six MMAs per (channel, K-step) form
 //     b0c0 + b0c1 + b1c0 + b0c2 + b1c1 + b2c0 (the omitted products are below
-//     2^-24 relative), accumulated in FP32 in tensor memory;
+//     2^-24 relative), accumulated in FP32 in tensor memory.  The tensor core
+//     truncates its FP32 accumulation, so every MMA into a large accumulator can
+//     lose up to an ulp of it; for the value channel (the one rho is built from)
+//     the leading b0c0 products of K-step k go to accumulator k mod 4 and the five
+//     small correction products to a fifth, and the five are summed in the
+//     epilogue.  Gradient channels use one accumulator each.
 //   * rho and grad rho accumulate the per-MO products in FP64.
 //
 // Tile: 128 grid points (the MMA's M), N = MO block padded to a multiple of 16
@@ -23,7 +28,8 @@
 // 128-byte swizzle atom of BF16).  Per chunk the CTA writes 4 channels x 3 parts
 // of A (128 x 64 BF16, K-major, SWIZZLE_128B) into shared memory, copies the
 // matching pre-split, pre-swizzled B block, and one thread issues 96 MMAs.
-// Accumulators: 4 channels x N FP32 columns of TMEM.  Persistent CTAs, one per SM.
+// Accumulators: 8 x N FP32 columns of TMEM (value: 4 leading + 1 correction;
+// d/dx, d/dy, d/dz).  Persistent CTAs, one per SM.
 #include <stdio.h>
 
 #include <cuda_bf16.h>
@@ -212,8 +218,8 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
     const int warp = tid >> 5;
     const int lane = tid & 31;
     const uint32_t bar_a = smem_u32(bar);
-    const int ncols = 4 * P.npad;
-    const uint32_t tm_cols = ncols <= 32 ? 32 : ncols <= 64 ? 64 : ncols <= 128 ? 128 : 256;
+    const int ncols = 8 * P.npad;
+    const uint32_t tm_cols = ncols <= 32 ? 32 : ncols <= 64 ? 64 : ncols <= 128 ? 128 : ncols <= 256 ? 256 : 512;
 
     // zero A once: padding columns are never written and must hold finite values
     for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)A_s)[i] = make_uint4(0, 0, 0, 0);
@@ -298,7 +304,6 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
                     const int bpart = P.npad * 128;
 #pragma unroll 1
                     for (int ch = 0; ch < 4; ++ch) {
-                        const uint32_t d = tmem + ch * P.npad;
 #pragma unroll
                         for (int k = 0; k < KC / 16; ++k) {
                             // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
@@ -308,8 +313,18 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
                             for (int t = 0; t < 6; ++t) {
                                 const uint64_t ad = sdesc(a0 + (ch * 3 + pa[t]) * A_TILE + k * 32);
                                 const uint64_t bd = sdesc(b0 + pb[t] * bpart + k * 32);
-                                const uint32_t acc = (c > 0 || k > 0 || t > 0) ? 1u : 0u;
-                                mma_bf16(d, ad, bd, idesc, acc);
+                                uint32_t col, acc;
+                                if (ch == 0 && t == 0) {         // leading product -> accumulator k
+                                    col = k;
+                                    acc = c > 0;
+                                } else if (ch == 0) {            // value corrections -> accumulator 4
+                                    col = 4;
+                                    acc = (c > 0 || k > 0 || t > 1);
+                                } else {                         // gradient channel ch -> accumulator 4 + ch
+                                    col = 4 + ch;
+                                    acc = (c > 0 || k > 0 || t > 0);
+                                }
+                                mma_bf16(tmem + col * P.npad, ad, bd, idesc, acc);
                             }
                         }
                     }
@@ -329,12 +344,18 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
                 const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
                 double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
                 for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
-                    float v0[8], v1[8], v2[8], v3[8];
+                    float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
                     tmem_ld8(tl + 0 * P.npad + m0, v0);
-                    tmem_ld8(tl + 1 * P.npad + m0, v1);
-                    tmem_ld8(tl + 2 * P.npad + m0, v2);
-                    tmem_ld8(tl + 3 * P.npad + m0, v3);
+                    tmem_ld8(tl + 1 * P.npad + m0, h1);
+                    tmem_ld8(tl + 2 * P.npad + m0, h2);
+                    tmem_ld8(tl + 3 * P.npad + m0, h3);
+                    tmem_ld8(tl + 4 * P.npad + m0, lo);
+                    tmem_ld8(tl + 5 * P.npad + m0, v1);
+                    tmem_ld8(tl + 6 * P.npad + m0, v2);
+                    tmem_ld8(tl + 7 * P.npad + m0, v3);
                     tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) v0[i] = ((v0[i] + h1[i]) + (h2[i] + h3[i])) + lo[i];
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const double o = __ldg(P.occ + pass * P.npad + m0 + i);

@@ -1,0 +1,95 @@
+"""Mixed-precision (tensor-core) rho and grad rho against the FP64 oracle.
+
+Error bar: max relative rho error <= 1e-6 over points with rho > 1e-10
+(orbkit_gb300.mixed.MIXED_RHO_RTOL / MIXED_RHO_FLOOR).  The gradient error,
+|grad - grad_ref| / (|grad_ref| + 1e-10), is bounded at 1e-3 here and reported
+by the benchmark.
+"""
+import numpy
+import pytest
+
+from helpers import load_golden
+
+pytestmark = pytest.mark.gpu
+
+GRAD_BAR = 1e-3
+
+
+@pytest.fixture(scope="module")
+def mixed():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from orbkit_gb300 import build
+    build.build()
+    from orbkit_gb300 import mixed as m
+    return m
+
+
+def _check(mixed, r, g, ro, go, what):
+    rep = mixed.error_report(r, g, ro, go)
+    assert rep["rho_max_rel"] <= mixed.MIXED_RHO_RTOL, (what, rep)
+    assert rep["grad_max_rel"] <= GRAD_BAR, (what, rep)
+    return rep
+
+
+def test_mixed_small_full_grid(mixed):
+    import okref
+    from orbkit_gb300 import synthetic
+    w = synthetic.small()
+    qc = w["qc"]
+    x, y, z = w["grid"]
+    r, g = mixed.rho_grad(qc, x, y, z, False)
+    pts = okref.grid2vector(x, y, z)
+    ro, go = okref.rho_threads(qc, *pts, drv=["x", "y", "z"], slice_length=4096)
+    _check(mixed, r, g, ro, go, "small 80^3")
+
+
+def test_mixed_mid_subgrid(mixed):
+    import okref
+    from orbkit_gb300 import synthetic
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    x, y, z = gx[40:72], gy[70:90], gz[50:70]
+    r, g = mixed.rho_grad(qc, x, y, z, False)
+    ro, go = okref.rho_threads(qc, *okref.grid2vector(x, y, z), drv=["x", "y", "z"], slice_length=512)
+    _check(mixed, r, g, ro, go, "mid block")
+
+
+def test_mixed_spherical_fg(mixed):
+    """Spherical basis with f and g shells and an 'N' factor (golden data of the reference)."""
+    qc, d = load_golden("sph_fg_N.npz")
+    x, y, z = d["points"]
+    r, g = mixed.rho_grad(qc, x, y, z, True)
+    _check(mixed, r, g, d["rho"], d["delta_rho"], "spherical")
+
+
+def test_mixed_many_mos_and_ragged(mixed):
+    """70 MOs (two MO passes of the kernel) on 1, 127, 128, 129 and 1000 points."""
+    import okref
+    from orbkit_gb300 import synthetic
+    rng = numpy.random.default_rng(7)
+    geo = synthetic.random_geometry(rng, 8, 9.0)
+    el = ["C", "O", "C", "H", "N", "H", "C", "H"]
+    ao = synthetic.build_basis(rng, el)
+    mo = synthetic.build_mos(rng, geo, ao, 70)
+    qc = synthetic.make_qc(geo, el, ao, mo)
+    for n in (1, 127, 128, 129, 1000):
+        p = rng.uniform(-5, 5, (3, n))
+        r, g = mixed.rho_grad(qc, p[0], p[1], p[2], True)
+        ro, go = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=128, nthreads=2)
+        _check(mixed, r, g, ro, go, "n=%d" % n)
+
+
+def test_mixed_cusp_points_use_fp64(mixed):
+    """Points within the cusp radius of a nucleus carry FP64 values."""
+    import okref
+    from orbkit_gb300 import synthetic
+    qc = synthetic.small()["qc"]
+    p = numpy.array(qc.geo_spec).T.copy()
+    p = numpy.concatenate([p, p + 0.05], axis=1)
+    r, g = mixed.rho_grad(qc, p[0], p[1], p[2], True)
+    ro, go = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=8, nthreads=1)
+    numpy.testing.assert_allclose(r, ro, rtol=1e-12)
+    numpy.testing.assert_allclose(g, go, rtol=1e-11, atol=1e-12 * numpy.abs(go).max())
