@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Benchmark: grid points/s for rho + grad rho on one GB300, mixed vs FP64 GPU path.
+
+Workload (default): the mid-size molecule -- 20 atoms (C/N/O/H 6:1:1:12) in a
+16-bohr box, 180 Cartesian AOs, 40 occupied MOs, regular 160^3 grid at 0.15 bohr
+(4 096 000 points) -- seeded synthetic data (orbkit_gb300.synthetic.mid).
+
+  value      points/s of the mixed-precision path (tensor-core contraction, FP64
+             exponent arguments and density accumulation, FP64 cusp region), inputs
+             resident in HBM, L2 flushed (256 MB write) between timed steps.
+  e2e        the same through the public evaluator with host buffers: every step
+             uploads geometry, primitives, MO coefficients, occupations and grid
+             vectors from pinned host memory and reads rho + grad back into pinned
+             host memory.
+  roofline   of the dominant kernel (the fused mixed kernel), achieved = algorithmic
+             contraction FLOPs (8 NMO NAO per point) / its CUDA-event launch time.
+  cpu_baseline  the CPU oracle (a C restatement of orbkit's cy_core/c_grid-based
+             path) on the host cores, on a bounded random sample of the grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun every rank evaluates its own copy of the workload (weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid points/s for rho+grad rho, mixed vs FP64 GPU path at stated max rel err"
+UNIT = "grid points/s"
+WORKLOAD = ("mid: 20 atoms (C/N/O/H 6:1:1:12, 16-bohr box), 180 Cartesian AOs (3s2p1d / 2s1p), "
+            "40 occupied MOs, regular 160^3 grid at 0.15 bohr, rho + grad rho")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel_key:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "50", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t is not None:
+                self.t.join(timeout=2)
+
+    def summary(self, t0, t1):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        window = [s for (t, s) in self.samples if t0 - 0.06 <= t <= t1 + 0.06] or [s for (_, s) in self.samples]
+        for s in window:
+            f = [v.strip() for v in s.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(numpy.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_rate(qc, gx, gy, gz, target_s=12.0, seed=0, max_pts=2_000_000):
+    """Oracle points/s on a random sample of the regular grid (all host threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import okref
+    okref.build()
+    cores = len(os.sched_getaffinity(0))
+    rng = numpy.random.default_rng(seed)
+
+    def sample(n):
+        idx = rng.integers(0, len(gx) * len(gy) * len(gz), n)
+        nyz = len(gy) * len(gz)
+        return gx[idx // nyz], gy[(idx // len(gz)) % len(gy)], gz[idx % len(gz)]
+
+    n0 = 64 * cores
+    x, y, z = sample(n0)
+    t = time.perf_counter()
+    okref.rho_threads(qc, x, y, z, drv=["x", "y", "z"], slice_length=64, nthreads=cores)
+    dt = time.perf_counter() - t
+    n = int(min(max_pts, max(n0, n0 / max(dt, 1e-6) * target_s)))
+    x, y, z = sample(n)
+    t = time.perf_counter()
+    okref.rho_threads(qc, x, y, z, drv=["x", "y", "z"], slice_length=max(64, n // (8 * cores)), nthreads=cores)
+    dt = time.perf_counter() - t
+    return n / dt, cores, n, dt
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    """The reference's CPU path for this workload: the C restatement of orbkit's
+    cy_core / c_grid-based grid path (rho + grad rho per slice, slices over all
+    host threads), bounded random samples of the same grid."""
+    rank, world, local = dist_setup(args)
+    if rank != 0:
+        return
+    from orbkit_gb300 import synthetic
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    rates = []
+    cores = n = None
+    for i in range(args.warmup + args.steps):
+        r, cores, n, dt = cpu_rate(qc, gx, gy, gz, target_s=args.ref_step_s, seed=i)
+        if i >= args.warmup:
+            rates.append((n, dt))
+    tot_n = sum(a for a, _ in rates)
+    tot_t = sum(b for _, b in rates)
+    value = tot_n / tot_t
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / len(rates),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "npts_per_step": n, "sample": "random grid points"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d random points of the 160^3 grid per step, rho + grad rho" % n},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from orbkit_gb300 import _lib, mixed, synthetic
+    from orbkit_gb300.core import _DeviceGrid
+
+    L = _lib.load()
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    npts = len(gx) * len(gy) * len(gz)
+    ev = mixed.MixedEvaluator(qc, device=dev)
+    b, plan = ev.basis, ev.plan
+    g = _DeviceGrid(gx, gy, gz, False, dev)
+    gd, keep = g.slice(0, npts)
+    rho = torch.empty(npts, dtype=torch.float64, device=dev)
+    grad = torch.empty((3, npts), dtype=torch.float64, device=dev)
+    r64 = torch.empty_like(rho)
+    g64 = torch.empty_like(grad)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    codes = _lib.int_array([1, 2, 3])
+    st = _lib.stream_handle()
+
+    def step_mixed():
+        ev.evaluate_device(g, rho, grad)
+
+    def step_fp64():
+        _lib.check(L.okg_rho(b.handle, gd, plan.nmo, _lib.ptr(plan.C), _lib.ptr(plan.occ), 3, codes, 0,
+                             _lib.ptr(r64), _lib.ptr(g64), npts, None, st))
+
+    def sync_all():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, k, w_):
+        for _ in range(w_):
+            fn()
+        sync_all()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        t0 = time.time()
+        for e0, e1 in evs:
+            flush.fill_(1)
+            e0.record()
+            fn()
+            e1.record()
+        sync_all()
+        t1 = time.time()
+        return sum(e0.elapsed_time(e1) for e0, e1 in evs) / k, t0, t1
+
+    # accuracy of the mixed path against the FP64 path (itself at 1e-12 of the oracle)
+    step_fp64()
+    step_mixed()
+    torch.cuda.synchronize()
+    ev.check()
+    err = mixed.error_report(rho.cpu().numpy(), grad.cpu().numpy(), r64.cpu().numpy(), g64.cpu().numpy())
+
+    fp64_ms, _, _ = timed(step_fp64, 2, 1)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ms, t0, t1 = timed(step_mixed, args.steps, args.warmup)
+    clocks.stop()
+    ev.check()
+    clk = clocks.summary(t0, t1)
+
+    # the dominant kernel alone (same stream as its launch: torch's current stream)
+    def kernel_only():
+        plan.rho(gd, rho, grad, npts)
+    kms, _, _ = timed(kernel_only, max(3, args.steps), 1)
+
+    # end to end through the evaluator with pinned host buffers
+    prim_h = torch.from_numpy(b.flat["prim"].copy()).pin_memory()
+    geo_h = torch.from_numpy(numpy.asarray(qc.geo_spec, dtype=numpy.float64).copy()).pin_memory()
+    C_h = torch.from_numpy(qc.mo_spec.get_coeffs()).pin_memory()
+    occ_h = torch.from_numpy(numpy.array([m["occ_num"] for m in qc.mo_spec])).pin_memory()
+    out_h = (torch.empty(npts, dtype=torch.float64).pin_memory(), torch.empty((3, npts), dtype=torch.float64).pin_memory())
+    gvec = [numpy.ascontiguousarray(v) for v in (gx, gy, gz)]
+
+    def step_e2e():
+        ev.update(geo=geo_h, prim=prim_h, coeffs=C_h, occ=occ_h)
+        ev.evaluate(*gvec, False, out=out_h)
+
+    for _ in range(args.warmup):
+        step_e2e()
+    sync_all()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    sync_all()
+    e2e_ms = (time.perf_counter() - te) * 1e3 / args.steps
+    h2d = (geo_h.numel() + prim_h.numel() + C_h.numel() + occ_h.numel() + sum(len(v) for v in gvec)) * 8
+    d2h = 4 * npts * 8
+
+    times = torch.tensor([ms, kms, e2e_ms, fp64_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    ms, kms, e2e_ms, fp64_ms = [float(v) for v in times.cpu()]
+    if rank != 0:
+        return
+
+    pk, pk_kind = peaks()
+    ncart, nmo = b.ncart, plan.nmo
+    flops = 8.0 * nmo * b.nao * npts
+    achieved = flops / (kms * 1e-3) / 1e12
+    fma = ctypes_fp64_rate(L)
+    fp64_path_fma_rate = 4.0 * nmo * ncart * npts / (fp64_ms * 1e-3)
+    n_fix = len(mixed.cusp_points_regular(qc.geo_spec, gx, gy, gz, ev.cusp_radius))
+    out = {
+        "metric": METRIC,
+        "value": world * npts / (ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD, "npts": npts, "nao": b.nao, "nmo": nmo, "path": "mixed",
+            "precision": "C.AO on tcgen05 with BF16x3 operand splits (6 MMAs), FP32 accumulation in TMEM; "
+                         "FP64 exponent arguments and density accumulation; points within %.2f bohr of a nucleus "
+                         "(%d points) recomputed in FP64" % (ev.cusp_radius, n_fix),
+            "max_rel_err": {"rho_max_rel": err["rho_max_rel"], "rho_floor": err["floor"],
+                            "rho_max_abs": err["rho_max_abs"], "grad_max_rel": err["grad_max_rel"],
+                            "against": "FP64 GPU path (1e-12 of the oracle)"},
+            "fp64_path": {"value": world * npts / (fp64_ms * 1e-3), "ms_per_step": fp64_ms,
+                          "fp64_fma_per_s_contraction": fp64_path_fma_rate},
+            "mixed_over_fp64": fp64_ms / ms,
+            "l2": "flushed between timed steps (256 MB device write)",
+            "parallelism": "weak: every GPU evaluates its own copy of the workload",
+        },
+        "roofline": {
+            "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / pk["bf16_tflops"], "traffic": profile_traffic("rho_mixed_kernel"),
+            "peak_source": "bf16 burst, %s (MEASURED_PEAKS.json)" % pk_kind if pk_kind == "measured" else pk_kind,
+            "kernel": "rho_mixed_kernel", "kernel_ms": kms,
+            "algorithmic": "8*NMO*NAO FLOP per point (value + 3 derivatives of C.AO)",
+            "hbm_bytes_per_point": 32, "hbm_gbs": 32.0 * npts / (kms * 1e-3) / 1e9, "hbm_peak_gbs": pk["hbm_gbs"],
+            "fp64_fma_peak_per_s": fma,
+        },
+        "clocks": clk,
+        "e2e": {"value": world * npts / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * (1 + (1 if n_fix else 0)),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        rate, cores, n, dt = cpu_rate(qc, gx, gy, gz)
+        out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "%d random points of the 160^3 grid, rho + grad rho, %.1f s" % (n, dt)}
+    print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_profile(args):
+    """Minimal launch sequence for ncu: each kernel of the path once as warm-up, then
+    once more (mixed kernel, FP64 fused kernel) on the full workload."""
+    import torch
+    from orbkit_gb300 import _lib, mixed, synthetic
+    from orbkit_gb300.core import _DeviceGrid
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    L = _lib.load()
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    npts = len(gx) * len(gy) * len(gz)
+    ev = mixed.MixedEvaluator(qc, device=dev)
+    g = _DeviceGrid(gx, gy, gz, False, dev)
+    gd, keep = g.slice(0, npts)
+    rho = torch.empty(npts, dtype=torch.float64, device=dev)
+    grad = torch.empty((3, npts), dtype=torch.float64, device=dev)
+    codes = _lib.int_array([1, 2, 3])
+    for _ in range(2):
+        ev.plan.rho(gd, rho, grad, npts)
+        _lib.check(L.okg_rho(ev.basis.handle, gd, ev.plan.nmo, _lib.ptr(ev.plan.C), _lib.ptr(ev.plan.occ), 3, codes,
+                             0, _lib.ptr(rho), _lib.ptr(grad), npts, None, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    ev.check()
+    print("profile run done: %d points" % npts)
+
+
+def ctypes_fp64_rate(L):
+    import ctypes
+    v = ctypes.c_double(0)
+    if L.okg_diag_fp64_fma_rate(4000, ctypes.byref(v)) != 0:
+        return None
+    return v.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-step-s", type=float, default=4.0)
+    ap.add_argument("--profile", action="store_true", help="minimal launch sequence for ncu captures")
+    args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

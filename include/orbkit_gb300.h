@@ -140,6 +140,10 @@ int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, dou
  * OKG_ERR_TIMEOUT if a wait expired since the last check (the word is then cleared). */
 int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
 
+/* Diagnostic (no counterpart in orbkit): measured FP64 FMA rate of the current device
+ * in FMA/s, from a kernel of independent FMA chains (synchronising; allocates). */
+int okg_diag_fp64_fma_rate(long long iters, double* fma_per_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,12 @@ SIGNATURES = {
                                    ctypes.c_int, _vp, ctypes.c_int64, _vp]),
     "okg_rho": (ctypes.c_int, [_vp, ctypes.POINTER(OkgGrid), ctypes.c_int, _vp, _vp, ctypes.c_int, _c_int_p,
                                ctypes.c_int, _vp, _vp, ctypes.c_int64, _vp, _vp]),
+    "okg_mixed_plan_create": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "okg_mixed_plan_destroy": (ctypes.c_int, [_vp]),
+    "okg_mixed_set_coeffs": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "okg_rho_mixed": (ctypes.c_int, [_vp, ctypes.POINTER(OkgGrid), ctypes.c_int, _vp, _vp, ctypes.c_int64, _vp]),
+    "okg_mixed_status": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
+    "okg_diag_fp64_fma_rate": (ctypes.c_int, [ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]),
 }
 
 

@@ -99,28 +99,83 @@ def cusp_points_regular(geo, x, y, z, radius):
     return numpy.unique(numpy.concatenate(out))
 
 
+class MixedEvaluator:
+    """Device resources for repeated mixed-precision rho / grad rho evaluation of
+    one molecule: the packed basis, the tensor-core coefficient plan and output
+    buffers.  ``update`` uploads new parameters from host arrays; ``evaluate``
+    takes a host grid and writes host outputs."""
+
+    def __init__(self, qc, cusp_radius=CUSP_RADIUS, device=None):
+        import torch
+        geo, ao_spec, mo_spec = unpack(qc)
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        self.basis = get_basis(geo, ao_spec, self.device)
+        occ = numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64)
+        self.plan = MixedPlan(self.basis, mo_spec.get_coeffs(), occ)
+        self.geo = numpy.asarray(geo, dtype=numpy.float64)
+        self.cusp_radius = cusp_radius
+        self._bufs = None
+
+    def update(self, geo=None, prim=None, coeffs=None, occ=None, stream=None):
+        """New nuclear positions / primitives / MO coefficients / occupations (host or device)."""
+        import torch
+        if geo is not None or prim is not None:
+            self.basis.set_params(geo=geo, prim=prim, stream=stream)
+            if geo is not None:
+                self.geo = (geo.cpu().numpy() if hasattr(geo, "cpu") else numpy.asarray(geo)).reshape(-1, 3)
+        if coeffs is not None or occ is not None:
+            p = self.plan
+            if coeffs is not None:
+                p.C = self.basis.c_eff(torch.as_tensor(coeffs, dtype=torch.float64).to(self.device, non_blocking=True))
+            if occ is not None:
+                p.occ = torch.as_tensor(occ, dtype=torch.float64).to(self.device, non_blocking=True).contiguous()
+            _lib.check(p._L.okg_mixed_set_coeffs(p.handle, _lib.ptr(p.C), _lib.ptr(p.occ), _lib.stream_handle(stream)))
+
+    def evaluate_device(self, g, rho=None, grad=None):
+        """Run on a _DeviceGrid; returns device tensors (rho, grad)."""
+        import torch
+        n = g.npts
+        if rho is None:
+            rho = torch.empty(n, dtype=torch.float64, device=self.device)
+            grad = torch.empty((3, n), dtype=torch.float64, device=self.device)
+        gd, keep = g.slice(0, n)
+        self.plan.rho(gd, rho, grad, n)
+        if self.cusp_radius and self.cusp_radius > 0:
+            fix_cusp(self.plan, self.geo, g, rho, grad, self.cusp_radius)
+        return rho, grad
+
+    def evaluate(self, x, y, z, is_vector, out=None):
+        """Host grid in, host (rho, grad) out.  `out` may hold preallocated (pinned)
+        host tensors (rho (npts,), grad (3, npts)) that receive the results."""
+        import torch
+        from .core import _DeviceGrid
+        g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
+                        numpy.asarray(z, dtype=numpy.float64), is_vector, self.device)
+        rho, grad = self.evaluate_device(g)
+        if out is not None:
+            out[0].copy_(rho, non_blocking=True)
+            out[1].copy_(grad, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            return out
+        return rho.cpu().numpy(), grad.cpu().numpy()
+
+    def check(self):
+        self.plan.check()
+
+
 def rho_grad(qc, x, y, z, is_vector, cusp_radius=CUSP_RADIUS, return_device=False):
     """rho and grad rho (3, npts) on the GPU mixed path, with the cusp region in FP64."""
-    import torch
     from .core import _DeviceGrid
-    geo, ao_spec, mo_spec = unpack(qc)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    b = get_basis(geo, ao_spec, dev)
-    occ = numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64)
-    plan = MixedPlan(b, mo_spec.get_coeffs(), occ)
-    g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
-                    numpy.asarray(z, dtype=numpy.float64), is_vector, dev)
-    n = g.npts
-    rho = torch.empty(n, dtype=torch.float64, device=dev)
-    grad = torch.empty((3, n), dtype=torch.float64, device=dev)
-    gd, keep = g.slice(0, n)
-    plan.rho(gd, rho, grad, n)
-    if cusp_radius and cusp_radius > 0:
-        fix_cusp(plan, geo, g, rho, grad, cusp_radius)
-    plan.check()
+    ev = MixedEvaluator(qc, cusp_radius)
     if return_device:
-        return rho, grad
-    return rho.cpu().numpy(), grad.cpu().numpy()
+        g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
+                        numpy.asarray(z, dtype=numpy.float64), is_vector, ev.device)
+        out = ev.evaluate_device(g)
+        ev.check()
+        return out
+    out = ev.evaluate(x, y, z, is_vector)
+    ev.check()
+    return out
 
 
 def fix_cusp(plan, geo, g, rho, grad, radius):
