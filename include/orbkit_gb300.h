@@ -140,6 +140,20 @@ int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, dou
  * OKG_ERR_TIMEOUT if a wait expired since the last check (the word is then cleared). */
 int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
 
+/* Allocation-free variant of okg_rho_mixed; no counterpart in orbkit.
+ * For callers that cannot allocate device memory where they evaluate the density
+ * (a framework that owns all device memory through its own pool, or a loop that
+ * cannot take cudaMalloc's implicit device synchronisation).  The MO coefficients
+ * d_coeff (C_eff, nmo x ncart) and occupations d_occ are split into a 2 MiB
+ * file-scope device array on every call instead of a plan's buffer; larger
+ * (basis, nmo) combinations return OKG_ERR_UNSUPPORTED.  The first call on a device
+ * looks up the array and sets up the kernel (make it before any stream capture).
+ * Calls that overlap on the GPU race on the shared array.  A tensor-core wait that
+ * expires sets *d_status to 1 (d_status may be NULL; the call clears it first). */
+int okg_rho_mixed_noalloc(const okg_basis* basis, const okg_grid* grid, int nmo, const double* d_coeff,
+                          const double* d_occ, int want_grad, double* d_rho, double* d_grad, int64_t ld,
+                          int* d_status, okg_stream stream);
+
 /* Diagnostic (no counterpart in orbkit): measured FP64 FMA rate of the current device
  * in FMA/s, from a kernel of independent FMA chains (synchronising; allocates). */
 int okg_diag_fp64_fma_rate(long long iters, double* fma_per_s);

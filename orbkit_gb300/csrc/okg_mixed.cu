@@ -572,3 +572,131 @@ extern "C" int okg_mixed_status(okg_mixed_plan* p, int* device_status)
     }
     return OKG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of okg_rho_mixed.
+//
+// Some callers cannot allocate device memory at the point where they evaluate the
+// density: code that runs inside a framework which owns all device memory through
+// its own pool, or a real-time loop that cannot pay the implicit device-wide
+// synchronisation of cudaMalloc/cudaFree.  They still need the tensor-core path
+// with fresh MO coefficients on every call, which normally goes through a plan
+// (okg_mixed_plan_create allocates the split-coefficient buffer).  This entry
+// point instead uses one file-scope device array as its scratch: the BF16 operand
+// tiles of the coefficients, the padded occupations and the timeout status word.
+//
+// * Limit: OKG_NOALLOC_SCRATCH_BYTES (2 MiB) of scratch per device; larger
+//   (basis, nmo) combinations are rejected with OKG_ERR_UNSUPPORTED.  Every GPU
+//   that loads the library holds the array until the process exits.
+// * The first call on a device looks up the array's device address
+//   (cudaGetSymbolAddress) and sets the kernel's shared-memory attribute, with that
+//   device current; make that first call before any stream capture.
+// * All calls on a device share the one array and it keeps the last call's
+//   contents: calls that overlap on the GPU (different streams, or host threads
+//   that do not order their streams) race on it.  Each call rewrites every byte it
+//   reads and clears the status word before its kernels run.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace okg {
+namespace mx {
+constexpr size_t NOALLOC_SCRATCH_BYTES = 2u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+struct NoallocDevice {
+    unsigned char* base = nullptr;  // device address of g_noalloc_scratch on this device
+    int sm_count = 0;
+    bool ready = false;
+};
+static NoallocDevice g_noalloc_dev[64];
+static std::mutex g_noalloc_mu;
+
+static size_t noalloc_smem() { return 1024 + A_BYTES + 3 * NMAX * 128 + 4 * M * 8 + 64; }
+}  // namespace mx
+}  // namespace okg
+
+extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int nmo, const double* d_coeff,
+                                     const double* d_occ, int want_grad, double* d_rho, double* d_grad, int64_t ld,
+                                     int* d_status, okg_stream stream)
+{
+    using namespace okg::mx;
+    if (!b || !gr || !d_coeff || !d_occ || !d_rho || (want_grad && !d_grad) || nmo <= 0)
+        return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: NULL argument or nmo <= 0");
+    Grid g;
+    g.x = gr->d_x;
+    g.y = gr->d_y;
+    g.z = gr->d_z;
+    g.npts = gr->npts;
+    g.offset = gr->offset;
+    g.nx = gr->nx;
+    g.ny = gr->ny;
+    g.nz = gr->nz;
+    g.regular = gr->regular;
+    if (g.npts < 0 || !g.x || !g.y || !g.z) return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: bad grid");
+    if (g.regular && (g.nx <= 0 || g.ny <= 0 || g.nz <= 0 || g.offset < 0 ||
+                      g.offset + g.npts > (long long)g.nx * g.ny * g.nz))
+        return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: regular grid range outside Nx*Ny*Nz");
+    if (ld < g.npts) return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: ld < npts");
+
+    // scratch layout: split coefficients | occupations | status word
+    const int npass = (nmo + NMAX - 1) / NMAX;
+    const int per = (nmo + npass - 1) / npass;
+    const int npad = (per + 15) / 16 * 16;
+    const size_t bpack_bytes = (size_t)npass * b->dev.nmchunk * 3 * npad * 128;
+    const size_t occ_off = (bpack_bytes + 255) & ~(size_t)255;
+    const size_t st_off = occ_off + (((size_t)npass * npad * 8 + 255) & ~(size_t)255);
+    if (st_off + 256 > NOALLOC_SCRATCH_BYTES)
+        return set_error(OKG_ERR_UNSUPPORTED,
+                         "okg_rho_mixed_noalloc: this basis and MO count need more than the 2 MiB of static "
+                         "scratch; use okg_mixed_plan_create / okg_rho_mixed");
+
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= 64) return set_error(OKG_ERR_DEVICE, "okg_rho_mixed_noalloc: device index above 63");
+    NoallocDevice* nd = &g_noalloc_dev[dev];
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!nd->ready) {
+            int major = 0, minor = 0, sms = 0;
+            cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+            cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (major != 10 || minor != 3) return set_error(OKG_ERR_DEVICE, "okg_rho_mixed_noalloc: needs an sm_103 GPU");
+            void* ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: cudaGetSymbolAddress");
+            e = cudaFuncSetAttribute(rho_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)noalloc_smem());
+            if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: shared memory attribute");
+            nd->base = (unsigned char*)ptr;
+            nd->sm_count = sms;
+            nd->ready = true;
+        }
+    }
+    if (g.npts == 0) return OKG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    __nv_bfloat16* bpack = (__nv_bfloat16*)nd->base;
+    double* occ = (double*)(nd->base + occ_off);
+    int* status = d_status ? d_status : (int*)(nd->base + st_off);
+    e = cudaMemsetAsync(status, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: clear status");
+    const BasisDev& B = b->dev;
+    pack_b_kernel<<<nd->sm_count * 4, 256, 0, st>>>(d_coeff, nmo, B.ncart, B.mcol_cart, B.nmchunk, npass, npad, bpack);
+    pack_occ_kernel<<<(npass * npad + 127) / 128, 128, 0, st>>>(d_occ, nmo, npass * npad, occ);
+    Params P;
+    P.B = B;
+    P.g = g;
+    P.bpack = (const uint4*)bpack;
+    P.occ = occ;
+    P.npass = npass;
+    P.npad = npad;
+    P.want_grad = want_grad;
+    P.rho = d_rho;
+    P.grad = d_grad;
+    P.ld = ld;
+    P.status = status;
+    P.ntiles = (g.npts + M - 1) / M;
+    const long long grid = P.ntiles < nd->sm_count ? P.ntiles : nd->sm_count;
+    rho_mixed_kernel<<<(unsigned)grid, NT, noalloc_smem(), st>>>(P);
+    return cuda_status(cudaGetLastError(), "okg_rho_mixed_noalloc launch");
+}
