@@ -67,14 +67,10 @@ def build(force=False, verbose=False, extra=()):
                 print(log)
     if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs + ["-lcuda"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            # libcuda may be absent on a build-only machine; the runtime does not need it at link time
-            cmd = [c for c in cmd if c != "-lcuda"]
-            r = subprocess.run(cmd, capture_output=True, text=True)
-            if r.returncode != 0:
-                raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
         os.replace(tmp, LIB)
     return LIB
 
