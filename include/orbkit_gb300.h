@@ -140,6 +140,24 @@ int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, dou
  * OKG_ERR_TIMEOUT if a wait expired since the last check (the word is then cleared). */
 int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
 
+/* ------------------------------------------------------------------- adjoint
+ * Gradients of a loss L(rho, grad rho) with respect to the MO coefficients, the
+ * primitive exponents and contraction coefficients, and the nuclear coordinates,
+ * given the cotangents d_g_rho = dL/drho (npts) and d_g_grad = dL/d(grad rho)
+ * (3 x ld, or NULL).  Differentiates the forward of okg_rho with codes {1,2,3}
+ * (orbkit/core.py:266-300; AO math of orbkit/c_grid-based.c:9-79 and
+ * orbkit/c_support.c:28-188); AO tiles are recomputed, not stored.
+ * Outputs (overwritten): d_dcoeff (nmo x ncart, w.r.t. C_eff), d_dprim (nprim x 2:
+ * d/dalpha, d/dc in ao_spec.get_prim_coeffs() order), d_dgeo (natom x 3).
+ * precision: 64 or 32 (arithmetic of the backward).  nmo <= 48.  d_work is caller
+ * memory of at least okg_rho_backward_workspace bytes (per-CTA partial sums,
+ * reduced in a fixed order: results are deterministic). */
+int okg_rho_backward_workspace(const okg_basis* basis, const okg_grid* grid, int nmo, int precision, size_t* bytes);
+int okg_rho_backward(const okg_basis* basis, const okg_grid* grid, int nmo, const double* d_coeff,
+                     const double* d_occ, const double* d_g_rho, const double* d_g_grad, int64_t ld, int precision,
+                     double* d_dcoeff, double* d_dprim, double* d_dgeo, void* d_work, size_t work_bytes,
+                     okg_stream stream);
+
 /* Allocation-free variant of okg_rho_mixed; no counterpart in orbkit.
  * For callers that cannot allocate device memory where they evaluate the density
  * (a framework that owns all device memory through its own pool, or a loop that

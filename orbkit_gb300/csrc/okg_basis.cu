@@ -41,15 +41,21 @@ static int dfact(int n) { return n <= 0 ? 1 : n * dfact(n - 2); }
 // the mixed path.
 __global__ void prim_weights_kernel(const double* __restrict__ prim_in, const int* __restrict__ prim_L, int nprim,
                                     int is_normalized, double* __restrict__ prim_out, float* __restrict__ prim32,
-                                    PrimMx* __restrict__ prim_mx)
+                                    PrimMx* __restrict__ prim_mx, double* __restrict__ prim_adj)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nprim) return;
     const double a = prim_in[2 * i];
     const double c = prim_in[2 * i + 1];
     const int L = prim_L[i];
-    double w = c;
-    if (!is_normalized) w = c * (pow(2.0 / M_PI, 0.75) * (pow(2.0, (double)L) * pow(a, (2.0 * L + 3.0) / 4.0)));
+    double w = c, nrm = 1.0, dw = 0.0;
+    if (!is_normalized) {
+        nrm = pow(2.0 / M_PI, 0.75) * (pow(2.0, (double)L) * pow(a, (2.0 * L + 3.0) / 4.0));
+        w = c * nrm;
+        dw = w * (2.0 * L + 3.0) / (4.0 * a);  // d w / d alpha
+    }
+    prim_adj[2 * i] = dw;
+    prim_adj[2 * i + 1] = nrm;
     prim_out[2 * i] = a;
     prim_out[2 * i + 1] = w;
     // mixed path: alpha * log2(e) and w as float hi + lo pairs
@@ -275,6 +281,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     const size_t o_scoef = lay.take(sizeof(double) * (sph_coef.size() + 1));
     const size_t o_chunks = lay.take(sizeof(int4) * chunks.size());
     const size_t o_pmx = lay.take(sizeof(PrimMx) * nprim);
+    const size_t o_padj = lay.take(sizeof(double) * 2 * nprim);
     const size_t o_cg32 = lay.take(sizeof(float) * comp_g32.size());
     const size_t o_mch = lay.take(sizeof(int4) * mchunks.size());
     const size_t o_mcc = lay.take(sizeof(int) * mcol_cart.size());
@@ -325,6 +332,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     d.sph_coef = (const double*)(blk + o_scoef);
     d.chunks = (const int4*)(blk + o_chunks);
     d.prim_mx = (const PrimMx*)(blk + o_pmx);
+    d.prim_adj = (const double*)(blk + o_padj);
     d.comp_g32 = (const float*)(blk + o_cg32);
     d.mchunks = (const int4*)(blk + o_mch);
     d.mcol_cart = (const int*)(blk + o_mcc);
@@ -378,6 +386,6 @@ extern "C" int okg_basis_set_params(okg_basis* b, const double* d_geo, const dou
     atoms_kernel<<<(b->natom + 127) / 128, 128, 0, st>>>(d_geo, b->natom, (double*)b->dev.atoms);
     prim_weights_kernel<<<(b->nprim + 127) / 128, 128, 0, st>>>(d_prim, b->prim_L, b->nprim, b->is_normalized,
                                                                  (double*)b->dev.prim, (float*)b->dev.prim32,
-                                                                 (PrimMx*)b->dev.prim_mx);
+                                                                 (PrimMx*)b->dev.prim_mx, (double*)b->dev.prim_adj);
     return cuda_status(cudaGetLastError(), "okg_basis_set_params");
 }

@@ -74,6 +74,7 @@ struct BasisDev {
     const double* sph_coef;  // coefficient x global factor
     const int4* chunks;      // nchunk x {first shell, end shell, first Cartesian row, end row}
     const PrimMx* prim_mx;   // nprim (mixed path)
+    const double* prim_adj;  // nprim x 2 : dw/dalpha, w/c (the alpha-dependent norm) for the adjoint
     const float* comp_g32;   // comp_g in FP32 (mixed path)
     const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= 64 columns)
     const int* mcol_cart;    // nmchunk x 64: listed Cartesian row feeding each column, or -1
