@@ -130,6 +130,10 @@ int okg_rho(const okg_basis* basis, const okg_grid* grid, int nmo, const double*
 typedef struct okg_mixed_plan okg_mixed_plan;
 /* Allocates the plan's device buffer (split coefficients, occupations, status word). */
 int okg_mixed_plan_create(const okg_basis* basis, int nmo, okg_mixed_plan** out);
+/* Same with the MMA's N tile (MO columns per pass over the AO chunks) limited to
+ * n_max (16, 32, 48 or 64; okg_mixed_plan_create uses 64): a tile shape for the
+ * autotuner -- fewer columns per pass, more passes. */
+int okg_mixed_plan_create_tiled(const okg_basis* basis, int nmo, int n_max, okg_mixed_plan** out);
 int okg_mixed_plan_destroy(okg_mixed_plan* plan);
 /* Split C_eff (nmo x ncart, FP64, device) into the BF16 operand tiles; copy occ (nmo). */
 int okg_mixed_set_coeffs(okg_mixed_plan* plan, const double* d_coeff, const double* d_occ, okg_stream stream);
@@ -139,6 +143,25 @@ int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, dou
 /* Synchronising check of the plan's device status word (bounded tensor-core waits):
  * OKG_ERR_TIMEOUT if a wait expired since the last check (the word is then cleared). */
 int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
+
+/* ------------------------------------------------------------------- batches
+ * Many molecules with uneven point sets (e.g. atom-centred grids) in one
+ * persistent launch of the mixed kernel: no counterpart in orbkit, which evaluates
+ * one molecule per call (orbkit/core.py:314); each molecule's result is what
+ * okg_rho_mixed gives for it.  The batch holds one (plan, grid, outputs) entry per
+ * molecule; tiles of 128 points are numbered across molecules in the given order
+ * and handed out to one CTA per SM through a device counter.  okg_batch_run is a
+ * counter reset plus one kernel launch on `stream` and can be captured in a CUDA
+ * graph.  okg_batch_set_schedule sets the tiles taken per counter increment and the
+ * number of CTAs (the autotuner's knobs). */
+typedef struct okg_batch okg_batch;
+int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* grids, double* const* d_rho,
+                     double* const* d_grad, const int64_t* ld, int want_grad, okg_batch** out);
+int okg_batch_destroy(okg_batch* batch);
+int okg_batch_set_schedule(okg_batch* batch, int tiles_per_grab, int ctas);
+int okg_batch_tiles(const okg_batch* batch, long long* total_tiles);
+int okg_batch_run(okg_batch* batch, okg_stream stream);
+int okg_batch_status(okg_batch* batch, int* device_status);
 
 /* ------------------------------------------------------------------- adjoint
  * Gradients of a loss L(rho, grad rho) with respect to the MO coefficients, the

@@ -34,6 +34,8 @@
 
 #include <cuda_bf16.h>
 
+#include <vector>
+
 #include "okg_internal.cuh"
 
 namespace okg {
@@ -202,30 +204,219 @@ __device__ __forceinline__ uint32_t sw128_off(int m, int k)
     return (uint32_t)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 3) ^ (m & 7)) & 7) << 4) + ((k & 7) << 1));
 }
 
-__global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
-{
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* A_s = smem;                            // 12 x 16 KB
-    unsigned char* B_s = smem + A_BYTES;                  // 3 x npad x 128 B
-    const int bbytes = 3 * P.npad * 128;
-    double* red = (double*)(B_s + 3 * NMAX * 128);        // 4 x 128 doubles
-    uint64_t* bar = (uint64_t*)(red + 4 * M);
-    uint32_t* tmem_slot = (uint32_t*)(bar + 1);
-    int* abort_flag = (int*)(tmem_slot + 1);
+// One molecule as seen by a tile: its basis tables, grid, coefficient tiles and outputs.
+struct MolDesc {
+    BasisDev B;
+    Grid g;
+    const uint4* bpack;  // [npass][nmchunk][3][npad x 128 B], pre-swizzled
+    const double* occ;   // [npass * npad], zero padded
+    double* rho;
+    double* grad;        // 3 x ld
+    long long ld;
+    long long tile0;     // first tile of this molecule in the batch's tile numbering
+    long long ntiles;
+    int npass, npad;
+    int want_grad;
+    int pad_;
+};
 
+// Shared-memory pieces of the CTA used by every tile.
+struct CtaState {
+    unsigned char* A_s;
+    unsigned char* B_s;
+    double* red;
+    uint32_t bar_a;
+    uint32_t tmem;
+    int* abort_flag;
+};
+
+// The whole computation of one 128-point tile of one molecule: per MO pass and
+// chunk, B copy + A generation + 96 MMAs, then the FP64 epilogue and the stores.
+__device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, const CtaState& S, uint32_t& phase,
+                                           int* status)
+{
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
     const int lane = tid & 31;
-    const uint32_t bar_a = smem_u32(bar);
-    const int ncols = 8 * P.npad;
-    const uint32_t tm_cols = ncols <= 32 ? 32 : ncols <= 64 ? 64 : ncols <= 128 ? 128 : ncols <= 256 ? 256 : 512;
+    const int prow = tid & (M - 1);  // point row of this thread in the tile
+    const int half = tid >> 7;       // generation: shells alternate between the two halves
+    const BasisDev& B = D.B;
+    const int npad = D.npad;
+    const uint32_t idesc = idesc_bf16(M, npad);
+    const int bbytes = 3 * npad * 128;
+    unsigned char* A_s = S.A_s;
+    unsigned char* B_s = S.B_s;
+    double* red = S.red;
 
-    // zero A once: padding columns are never written and must hold finite values
-    for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)A_s)[i] = make_uint4(0, 0, 0, 0);
+    const long long p = tile * M + prow;
+    const bool valid = p < D.g.npts;
+    double x, y, z;
+    grid_point(D.g, valid ? p : D.g.npts - 1, x, y, z);
+    double rho_acc = 0.0, gx_acc = 0.0, gy_acc = 0.0, gz_acc = 0.0;
+
+    for (int pass = 0; pass < D.npass; ++pass) {
+        for (int c = 0; c < B.nmchunk; ++c) {
+            if (c > 0) {  // previous chunk's MMAs must be done before A/B are overwritten
+                if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
+                phase ^= 1;
+            }
+            // B block of this (pass, chunk)
+            const uint4* src = D.bpack + ((long long)pass * B.nmchunk + c) * (bbytes / 16);
+            for (int i = tid; i < bbytes / 16; i += NT) ((uint4*)B_s)[i] = src[i];
+            // A: AO values of this chunk's shells for this thread's point
+            const int4 ck = B.mchunks[c];
+            int last_atom = -1;
+            double X = 0, Y = 0, Z = 0, rr = 0;
+            float Xf = 0, Yf = 0, Zf = 0;
+            for (int s = ck.x + half; s < ck.y; s += 2) {
+                const Shell sh = B.shells[s];
+                if (sh.atom != last_atom) {
+                    X = x - B.atoms[4 * sh.atom];
+                    Y = y - B.atoms[4 * sh.atom + 1];
+                    Z = z - B.atoms[4 * sh.atom + 2];
+                    rr = X * X + Y * Y + Z * Z;
+                    Xf = (float)X;
+                    Yf = (float)Y;
+                    Zf = (float)Z;
+                    last_atom = sh.atom;
+                }
+                float R0 = 0.f, R1 = 0.f;
+                for (int q = 0; q < sh.nprim; ++q) {
+                    const PrimMx pm = B.prim_mx[sh.prim0 + q];
+                    const float e = exp2_neg(pm.a2 * rr);
+                    R0 = fmaf(pm.w, e, R0);
+                    R1 = fmaf(pm.wa, e, R1);
+                }
+                const Radial<float> r{R0, R1, 0.f};
+                shell_eval_L(sh.L, Xf, Yf, Zf, r, 0xFu, false, [&](int ch, int j, float v) {
+                    v *= B.comp_g32[sh.comp0 + j];
+                    __nv_bfloat16 b0, b1, b2;
+                    split3(v, b0, b1, b2);
+                    const uint32_t off = sw128_off(prow, sh.mcol + j);
+                    unsigned char* base = A_s + ch * 3 * A_TILE + off;
+                    *(__nv_bfloat16*)(base) = b0;
+                    *(__nv_bfloat16*)(base + A_TILE) = b1;
+                    *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
+                });
+            }
+            fence_proxy_async();
+            __syncthreads();
+            if (tid == 0 && !*S.abort_flag) {
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(A_s), b0 = smem_u32(B_s);
+                const int bpart = npad * 128;
+#pragma unroll 1
+                for (int ch = 0; ch < 4; ++ch) {
+#pragma unroll
+                    for (int k = 0; k < KC / 16; ++k) {
+                        // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
+                        const int pa[6] = {0, 0, 1, 0, 1, 2};
+                        const int pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+                        for (int t = 0; t < 6; ++t) {
+                            const uint64_t ad = sdesc(a0 + (ch * 3 + pa[t]) * A_TILE + k * 32);
+                            const uint64_t bd = sdesc(b0 + pb[t] * bpart + k * 32);
+                            uint32_t col, acc;
+                            if (ch == 0 && t == 0) {         // leading product -> accumulator k
+                                col = k;
+                                acc = c > 0;
+                            } else if (ch == 0) {            // value corrections -> accumulator 4
+                                col = 4;
+                                acc = (c > 0 || k > 0 || t > 1);
+                            } else {                         // gradient channel ch -> accumulator 4 + ch
+                                col = 4 + ch;
+                                acc = (c > 0 || k > 0 || t > 0);
+                            }
+                            mma_bf16(S.tmem + col * npad, ad, bd, idesc, acc);
+                        }
+                    }
+                }
+                mma_commit(S.bar_a);
+            } else if (tid == 0) {
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(S.bar_a) : "memory");
+            }
+        }
+        // accumulators of this pass complete
+        if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
+        phase ^= 1;
+        tc_fence_after();
+        // epilogue: warp w reads TMEM lanes 32*(w%4).. (its 32 points), MO half w/4
+        {
+            const int q = warp & 3, h = warp >> 2;
+            const int nh = npad / 2;
+            const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
+            double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
+            for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
+                float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
+                tmem_ld8(tl + 0 * npad + m0, v0);
+                tmem_ld8(tl + 1 * npad + m0, h1);
+                tmem_ld8(tl + 2 * npad + m0, h2);
+                tmem_ld8(tl + 3 * npad + m0, h3);
+                tmem_ld8(tl + 4 * npad + m0, lo);
+                tmem_ld8(tl + 5 * npad + m0, v1);
+                tmem_ld8(tl + 6 * npad + m0, v2);
+                tmem_ld8(tl + 7 * npad + m0, v3);
+                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v0[i] = ((v0[i] + h1[i]) + (h2[i] + h3[i])) + lo[i];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const double o = __ldg(D.occ + pass * npad + m0 + i);
+                    racc = fma(o, (double)(v0[i] * v0[i]), racc);
+                    const double o2 = 2.0 * o;
+                    ga = fma(o2, (double)(v0[i] * v1[i]), ga);
+                    gb = fma(o2, (double)(v0[i] * v2[i]), gb);
+                    gc = fma(o2, (double)(v0[i] * v3[i]), gc);
+                }
+            }
+            const int pt = 32 * q + lane;
+            if (h == 1) {
+                red[pt] = racc;
+                red[M + pt] = ga;
+                red[2 * M + pt] = gb;
+                red[3 * M + pt] = gc;
+            }
+            tc_fence_before();
+            __syncthreads();
+            if (h == 0) {
+                // warp w < 4, lane l: point 32 w + l == tid of this tile
+                rho_acc += racc + red[pt];
+                gx_acc += ga + red[M + pt];
+                gy_acc += gb + red[2 * M + pt];
+                gz_acc += gc + red[3 * M + pt];
+            }
+            __syncthreads();
+            tc_fence_after();
+        }
+    }
+    if (tid < M && valid && !*S.abort_flag) {
+        D.rho[p] = rho_acc;
+        if (D.want_grad) {
+            D.grad[p] = gx_acc;
+            D.grad[D.ld + p] = gy_acc;
+            D.grad[2 * D.ld + p] = gz_acc;
+        }
+    }
+}
+
+// CTA set-up shared by the kernels: shared-memory carve-up, A zeroed (padding
+// columns must hold finite values), mbarrier, TMEM allocation (all 512 columns
+// when `cols` is 512).
+__device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_cols)
+{
+    const int tid = threadIdx.x, warp = tid >> 5;
+    CtaState S;
+    S.A_s = smem;
+    S.B_s = smem + A_BYTES;
+    S.red = (double*)(S.B_s + 3 * NMAX * 128);
+    uint64_t* bar = (uint64_t*)(S.red + 4 * M);
+    uint32_t* tmem_slot = (uint32_t*)(bar + 1);
+    S.abort_flag = (int*)(tmem_slot + 1);
+    S.bar_a = smem_u32(bar);
+    for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        mbar_init(bar_a, 1);
-        *abort_flag = 0;
+        mbar_init(S.bar_a, 1);
+        *S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -237,174 +428,100 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-    uint32_t phase = 0;
-    const uint32_t idesc = idesc_bf16(M, P.npad);
-    const int prow = tid & (M - 1);  // point row of this thread in the tile
-    const int half = tid >> 7;       // generation: shells alternate between the two halves
-    const BasisDev& B = P.B;
+    S.tmem = *tmem_slot;
+    return S;
+}
 
-    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
-        const long long p = tile * M + prow;
-        const bool valid = p < P.g.npts;
-        double x, y, z;
-        grid_point(P.g, valid ? p : P.g.npts - 1, x, y, z);
-        double rho_acc = 0.0, gx_acc = 0.0, gy_acc = 0.0, gz_acc = 0.0;
-
-        for (int pass = 0; pass < P.npass; ++pass) {
-            for (int c = 0; c < B.nmchunk; ++c) {
-                if (c > 0) {  // previous chunk's MMAs must be done before A/B are overwritten
-                    if (!mbar_wait(bar_a, phase, P.status)) *abort_flag = 1;
-                    phase ^= 1;
-                }
-                // B block of this (pass, chunk)
-                const uint4* src = P.bpack + ((long long)pass * B.nmchunk + c) * (bbytes / 16);
-                for (int i = tid; i < bbytes / 16; i += NT) ((uint4*)B_s)[i] = src[i];
-                // A: AO values of this chunk's shells for this thread's point
-                const int4 ck = B.mchunks[c];
-                int last_atom = -1;
-                double X = 0, Y = 0, Z = 0, rr = 0;
-                float Xf = 0, Yf = 0, Zf = 0;
-                for (int s = ck.x + half; s < ck.y; s += 2) {
-                    const Shell sh = B.shells[s];
-                    if (sh.atom != last_atom) {
-                        X = x - B.atoms[4 * sh.atom];
-                        Y = y - B.atoms[4 * sh.atom + 1];
-                        Z = z - B.atoms[4 * sh.atom + 2];
-                        rr = X * X + Y * Y + Z * Z;
-                        Xf = (float)X;
-                        Yf = (float)Y;
-                        Zf = (float)Z;
-                        last_atom = sh.atom;
-                    }
-                    float R0 = 0.f, R1 = 0.f;
-                    for (int q = 0; q < sh.nprim; ++q) {
-                        const PrimMx pm = B.prim_mx[sh.prim0 + q];
-                        const float e = exp2_neg(pm.a2 * rr);
-                        R0 = fmaf(pm.w, e, R0);
-                        R1 = fmaf(pm.wa, e, R1);
-                    }
-                    const Radial<float> r{R0, R1, 0.f};
-                    shell_eval_L(sh.L, Xf, Yf, Zf, r, 0xFu, false, [&](int ch, int j, float v) {
-                        v *= B.comp_g32[sh.comp0 + j];
-                        __nv_bfloat16 b0, b1, b2;
-                        split3(v, b0, b1, b2);
-                        const uint32_t off = sw128_off(prow, sh.mcol + j);
-                        unsigned char* base = A_s + ch * 3 * A_TILE + off;
-                        *(__nv_bfloat16*)(base) = b0;
-                        *(__nv_bfloat16*)(base + A_TILE) = b1;
-                        *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
-                    });
-                }
-                fence_proxy_async();
-                __syncthreads();
-                if (tid == 0 && !*abort_flag) {
-                    tc_fence_after();
-                    const uint32_t a0 = smem_u32(A_s), b0 = smem_u32(B_s);
-                    const int bpart = P.npad * 128;
-#pragma unroll 1
-                    for (int ch = 0; ch < 4; ++ch) {
-#pragma unroll
-                        for (int k = 0; k < KC / 16; ++k) {
-                            // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
-                            const int pa[6] = {0, 0, 1, 0, 1, 2};
-                            const int pb[6] = {0, 1, 0, 2, 1, 0};
-#pragma unroll
-                            for (int t = 0; t < 6; ++t) {
-                                const uint64_t ad = sdesc(a0 + (ch * 3 + pa[t]) * A_TILE + k * 32);
-                                const uint64_t bd = sdesc(b0 + pb[t] * bpart + k * 32);
-                                uint32_t col, acc;
-                                if (ch == 0 && t == 0) {         // leading product -> accumulator k
-                                    col = k;
-                                    acc = c > 0;
-                                } else if (ch == 0) {            // value corrections -> accumulator 4
-                                    col = 4;
-                                    acc = (c > 0 || k > 0 || t > 1);
-                                } else {                         // gradient channel ch -> accumulator 4 + ch
-                                    col = 4 + ch;
-                                    acc = (c > 0 || k > 0 || t > 0);
-                                }
-                                mma_bf16(tmem + col * P.npad, ad, bd, idesc, acc);
-                            }
-                        }
-                    }
-                    mma_commit(bar_a);
-                } else if (tid == 0) {
-                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_a) : "memory");
-                }
-            }
-            // accumulators of this pass complete
-            if (!mbar_wait(bar_a, phase, P.status)) *abort_flag = 1;
-            phase ^= 1;
-            tc_fence_after();
-            // epilogue: warp w reads TMEM lanes 32*(w%4).. (its 32 points), MO half w/4
-            {
-                const int q = warp & 3, h = warp >> 2;
-                const int nh = P.npad / 2;
-                const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
-                double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
-                for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
-                    float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
-                    tmem_ld8(tl + 0 * P.npad + m0, v0);
-                    tmem_ld8(tl + 1 * P.npad + m0, h1);
-                    tmem_ld8(tl + 2 * P.npad + m0, h2);
-                    tmem_ld8(tl + 3 * P.npad + m0, h3);
-                    tmem_ld8(tl + 4 * P.npad + m0, lo);
-                    tmem_ld8(tl + 5 * P.npad + m0, v1);
-                    tmem_ld8(tl + 6 * P.npad + m0, v2);
-                    tmem_ld8(tl + 7 * P.npad + m0, v3);
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) v0[i] = ((v0[i] + h1[i]) + (h2[i] + h3[i])) + lo[i];
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const double o = __ldg(P.occ + pass * P.npad + m0 + i);
-                        racc = fma(o, (double)(v0[i] * v0[i]), racc);
-                        const double o2 = 2.0 * o;
-                        ga = fma(o2, (double)(v0[i] * v1[i]), ga);
-                        gb = fma(o2, (double)(v0[i] * v2[i]), gb);
-                        gc = fma(o2, (double)(v0[i] * v3[i]), gc);
-                    }
-                }
-                const int pt = 32 * q + lane;
-                if (h == 1) {
-                    red[pt] = racc;
-                    red[M + pt] = ga;
-                    red[2 * M + pt] = gb;
-                    red[3 * M + pt] = gc;
-                }
-                tc_fence_before();
-                __syncthreads();
-                if (h == 0) {
-                    // this thread owns point pt of the tile for the output
-                    racc += red[pt];
-                    ga += red[M + pt];
-                    gb += red[2 * M + pt];
-                    gc += red[3 * M + pt];
-                    // point pt belongs to thread pt (tid < 128 <=> h == 0 for warps 0..3)
-                    rho_acc += racc;
-                    gx_acc += ga;
-                    gy_acc += gb;
-                    gz_acc += gc;
-                }
-                __syncthreads();
-                tc_fence_after();
-            }
-        }
-        // threads 0..127 hold the totals of point tid (warp w<4, lane l -> point 32w + l == tid)
-        if (tid < M && valid && !*abort_flag) {
-            P.rho[p] = rho_acc;
-            if (P.want_grad) {
-                P.grad[p] = gx_acc;
-                P.grad[P.ld + p] = gy_acc;
-                P.grad[2 * P.ld + p] = gz_acc;
-            }
-        }
-        if (*abort_flag) break;
-    }
+__device__ __forceinline__ void cta_teardown(const CtaState& S, uint32_t tm_cols)
+{
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tm_cols));
+    if ((threadIdx.x >> 5) == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(tm_cols));
+}
+
+__host__ __device__ inline uint32_t tmem_cols_for(int npad)
+{
+    const int n = 8 * npad;
+    return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
+}
+
+extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
+
+__global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
+{
+    unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t tm_cols = tmem_cols_for(P.npad);
+    CtaState S = cta_setup(smem, tm_cols);
+    MolDesc D;
+    D.B = P.B;
+    D.g = P.g;
+    D.bpack = P.bpack;
+    D.occ = P.occ;
+    D.rho = P.rho;
+    D.grad = P.grad;
+    D.ld = P.ld;
+    D.tile0 = 0;
+    D.ntiles = P.ntiles;
+    D.npass = P.npass;
+    D.npad = P.npad;
+    D.want_grad = P.want_grad;
+    uint32_t phase = 0;
+    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+        mixed_tile(D, tile, S, phase, P.status);
+        if (*S.abort_flag) break;
+    }
+    cta_teardown(S, tm_cols);
+}
+
+// Batched launch: one persistent CTA per SM takes `grab` consecutive tiles of
+// the concatenated tile numbering at a time from a global counter (zeroed before
+// the launch), finds the molecule by binary search over tile0 and copies its
+// descriptor to shared memory when the molecule changes.
+struct BatchParams {
+    const MolDesc* descs;  // nmol, ascending tile0
+    int nmol;
+    int grab;
+    long long total_tiles;
+    unsigned long long* counter;
+    int* status;
+};
+
+__global__ void __launch_bounds__(NT, 1) rho_mixed_batch_kernel(const BatchParams P)
+{
+    unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
+    CtaState S = cta_setup(smem, 512);
+    __shared__ MolDesc Dsh;
+    __shared__ long long work;
+    __shared__ int cur_mol;
+    if (threadIdx.x == 0) cur_mol = -1;
+    uint32_t phase = 0;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) work = (long long)atomicAdd(P.counter, (unsigned long long)P.grab);
+        __syncthreads();
+        const long long t0 = work;
+        if (t0 >= P.total_tiles || *S.abort_flag) break;
+        const long long t1 = t0 + P.grab < P.total_tiles ? t0 + P.grab : P.total_tiles;
+        for (long long t = t0; t < t1; ++t) {
+            __syncthreads();  // every thread is done with the previous tile's descriptor
+            if (threadIdx.x == 0) {
+                int lo = 0, hi = P.nmol - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (P.descs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+                }
+                if (lo != cur_mol) {
+                    Dsh = P.descs[lo];
+                    cur_mol = lo;
+                }
+            }
+            __syncthreads();
+            mixed_tile(Dsh, t - Dsh.tile0, S, phase, P.status);
+            if (*S.abort_flag) break;
+        }
+    }
+    cta_teardown(S, 512);
 }
 
 // Split C_eff (nmo x ncart, FP64) into three BF16 parts in the B operand layout:
@@ -460,9 +577,18 @@ struct okg_mixed_plan {
     size_t smem;
 };
 
+extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_max, okg_mixed_plan** out);
+
 extern "C" int okg_mixed_plan_create(const okg_basis* b, int nmo, okg_mixed_plan** out)
 {
+    return okg_mixed_plan_create_tiled(b, nmo, mx::NMAX, out);
+}
+
+extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_max, okg_mixed_plan** out)
+{
     if (!out || !b || nmo <= 0) return set_error(OKG_ERR_ARG, "okg_mixed_plan_create: NULL basis/out or nmo <= 0");
+    if (n_max < 16 || n_max > mx::NMAX || n_max % 16)
+        return set_error(OKG_ERR_ARG, "okg_mixed_plan_create_tiled: n_max must be 16, 32, 48 or 64");
     *out = nullptr;
     int dev = 0, major = 0, minor = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -474,7 +600,7 @@ extern "C" int okg_mixed_plan_create(const okg_basis* b, int nmo, okg_mixed_plan
     if (!p) return set_error(OKG_ERR_ALLOC, "okg_mixed_plan_create: host allocation");
     p->basis = b;
     p->nmo = nmo;
-    p->npass = (nmo + mx::NMAX - 1) / mx::NMAX;
+    p->npass = (nmo + n_max - 1) / n_max;
     const int per = (nmo + p->npass - 1) / p->npass;
     p->npad = (per + 15) / 16 * 16;
     p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * 128;
@@ -557,6 +683,150 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     const long long grid = P.ntiles < p->sm_count ? P.ntiles : p->sm_count;
     mx::rho_mixed_kernel<<<(unsigned)grid, mx::NT, p->smem, (cudaStream_t)stream>>>(P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
+}
+
+struct okg_batch {
+    int nmol;
+    void* block;              // descriptors | counter | status
+    mx::MolDesc* d_descs;
+    unsigned long long* d_counter;
+    int* d_status;
+    long long total_tiles;
+    int sm_count;
+    int grab;
+    int ctas;
+    size_t smem;
+};
+
+extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* grids, double* const* d_rho,
+                                double* const* d_grad, const int64_t* ld, int want_grad, okg_batch** out)
+{
+    if (!out || nmol <= 0 || !plans || !grids || !d_rho || !ld || (want_grad && !d_grad))
+        return set_error(OKG_ERR_ARG, "okg_batch_create: NULL argument or nmol <= 0");
+    *out = nullptr;
+    std::vector<mx::MolDesc> descs(nmol);
+    long long tile0 = 0;
+    int sms = 0;
+    for (int m = 0; m < nmol; ++m) {
+        const okg_mixed_plan* p = plans[m];
+        const okg_grid* gr = &grids[m];
+        if (!p || !d_rho[m] || (want_grad && !d_grad[m]) || gr->npts < 0 || !gr->d_x || !gr->d_y || !gr->d_z)
+            return set_error(OKG_ERR_ARG, "okg_batch_create: molecule with NULL plan, grid or output");
+        if (gr->regular && (gr->nx <= 0 || gr->ny <= 0 || gr->nz <= 0 || gr->offset < 0 ||
+                            gr->offset + gr->npts > (long long)gr->nx * gr->ny * gr->nz))
+            return set_error(OKG_ERR_ARG, "okg_batch_create: regular grid range outside Nx*Ny*Nz");
+        if (ld[m] < gr->npts) return set_error(OKG_ERR_ARG, "okg_batch_create: ld < npts");
+        mx::MolDesc& D = descs[m];
+        D.B = p->basis->dev;
+        D.g.x = gr->d_x;
+        D.g.y = gr->d_y;
+        D.g.z = gr->d_z;
+        D.g.npts = gr->npts;
+        D.g.offset = gr->offset;
+        D.g.nx = gr->nx;
+        D.g.ny = gr->ny;
+        D.g.nz = gr->nz;
+        D.g.regular = gr->regular;
+        D.bpack = (const uint4*)p->bpack;
+        D.occ = p->occ;
+        D.rho = d_rho[m];
+        D.grad = want_grad ? d_grad[m] : nullptr;
+        D.ld = ld[m];
+        D.ntiles = (gr->npts + mx::M - 1) / mx::M;
+        D.tile0 = tile0;
+        D.npass = p->npass;
+        D.npad = p->npad;
+        D.want_grad = want_grad;
+        D.pad_ = 0;
+        tile0 += D.ntiles;
+        sms = p->sm_count;
+    }
+    okg_batch* b = (okg_batch*)calloc(1, sizeof(okg_batch));
+    if (!b) return set_error(OKG_ERR_ALLOC, "okg_batch_create: host allocation");
+    const size_t dbytes = sizeof(mx::MolDesc) * nmol;
+    const size_t c_off = (dbytes + 255) & ~(size_t)255;
+    cudaError_t e = cudaMalloc(&b->block, c_off + 256);
+    if (e == cudaSuccess) e = cudaMemcpy(b->block, descs.data(), dbytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset((char*)b->block + c_off, 0, 256);
+    if (e != cudaSuccess) {
+        if (b->block) cudaFree(b->block);
+        free(b);
+        return cuda_status(e, "okg_batch_create: device descriptors");
+    }
+    b->nmol = nmol;
+    b->d_descs = (mx::MolDesc*)b->block;
+    b->d_counter = (unsigned long long*)((char*)b->block + c_off);
+    b->d_status = (int*)((char*)b->block + c_off + 64);
+    b->total_tiles = tile0;
+    b->sm_count = sms > 0 ? sms : 1;
+    b->grab = 1;
+    b->ctas = b->sm_count;
+    b->smem = 1024 + mx::A_BYTES + 3 * mx::NMAX * 128 + 4 * mx::M * 8 + 64;
+    e = cudaFuncSetAttribute(mx::rho_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    if (e != cudaSuccess) {
+        cudaFree(b->block);
+        free(b);
+        return cuda_status(e, "okg_batch_create: shared memory attribute");
+    }
+    *out = b;
+    return OKG_OK;
+}
+
+extern "C" int okg_batch_destroy(okg_batch* b)
+{
+    if (!b) return OKG_OK;
+    cudaError_t e = cudaFree(b->block);
+    free(b);
+    return cuda_status(e, "okg_batch_destroy");
+}
+
+extern "C" int okg_batch_set_schedule(okg_batch* b, int grab, int ctas)
+{
+    if (!b || grab < 1 || ctas < 1) return set_error(OKG_ERR_ARG, "okg_batch_set_schedule: grab and ctas >= 1");
+    if (ctas > b->sm_count) return set_error(OKG_ERR_UNSUPPORTED, "okg_batch_set_schedule: one CTA per SM at most");
+    b->grab = grab;
+    b->ctas = ctas;
+    return OKG_OK;
+}
+
+extern "C" int okg_batch_tiles(const okg_batch* b, long long* total_tiles)
+{
+    if (!b || !total_tiles) return set_error(OKG_ERR_ARG, "okg_batch_tiles: NULL argument");
+    *total_tiles = b->total_tiles;
+    return OKG_OK;
+}
+
+extern "C" int okg_batch_run(okg_batch* b, okg_stream stream)
+{
+    if (!b) return set_error(OKG_ERR_ARG, "okg_batch_run: NULL batch");
+    if (b->total_tiles == 0) return OKG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return cuda_status(e, "okg_batch_run: counter reset");
+    mx::BatchParams P;
+    P.descs = b->d_descs;
+    P.nmol = b->nmol;
+    P.grab = b->grab;
+    P.total_tiles = b->total_tiles;
+    P.counter = b->d_counter;
+    P.status = b->d_status;
+    const long long grid = b->total_tiles < b->ctas ? b->total_tiles : b->ctas;
+    mx::rho_mixed_batch_kernel<<<(unsigned)grid, mx::NT, b->smem, st>>>(P);
+    return cuda_status(cudaGetLastError(), "okg_batch_run launch");
+}
+
+extern "C" int okg_batch_status(okg_batch* b, int* device_status)
+{
+    if (!b || !device_status) return set_error(OKG_ERR_ARG, "okg_batch_status: NULL argument");
+    int v = 0;
+    cudaError_t e = cudaMemcpy(&v, b->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e, "okg_batch_status");
+    *device_status = v;
+    if (v) {
+        cudaMemset(b->d_status, 0, sizeof(int));
+        return set_error(OKG_ERR_TIMEOUT, "okg_batch_run: a tensor-core wait timed out");
+    }
+    return OKG_OK;
 }
 
 extern "C" int okg_mixed_status(okg_mixed_plan* p, int* device_status)
