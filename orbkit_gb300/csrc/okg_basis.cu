@@ -73,6 +73,25 @@ __global__ void prim_weights_kernel(const double* __restrict__ prim_in, const in
     prim_mx[i] = m;
 }
 
+// Mixed path: order each shell's primitives by ascending exponent, so that a
+// tile keeps a prefix of them when screening (the radial sums do not depend on
+// the order).  One thread per shell, insertion sort (a handful of primitives).
+__global__ void sort_prim_mx_kernel(const Shell* __restrict__ shells, int nshell, PrimMx* __restrict__ prim_mx)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nshell) return;
+    const int p0 = shells[s].prim0, np = shells[s].nprim;
+    for (int i = 1; i < np; ++i) {
+        const PrimMx v = prim_mx[p0 + i];
+        int j = i - 1;
+        while (j >= 0 && prim_mx[p0 + j].a2 > v.a2) {
+            prim_mx[p0 + j + 1] = prim_mx[p0 + j];
+            --j;
+        }
+        prim_mx[p0 + j + 1] = v;
+    }
+}
+
 __global__ void atoms_kernel(const double* __restrict__ geo, int natom, double* __restrict__ atoms)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -387,5 +406,6 @@ extern "C" int okg_basis_set_params(okg_basis* b, const double* d_geo, const dou
     prim_weights_kernel<<<(b->nprim + 127) / 128, 128, 0, st>>>(d_prim, b->prim_L, b->nprim, b->is_normalized,
                                                                  (double*)b->dev.prim, (float*)b->dev.prim32,
                                                                  (PrimMx*)b->dev.prim_mx, (double*)b->dev.prim_adj);
+    sort_prim_mx_kernel<<<(b->nshell + 127) / 128, 128, 0, st>>>(b->dev.shells, b->nshell, (PrimMx*)b->dev.prim_mx);
     return cuda_status(cudaGetLastError(), "okg_basis_set_params");
 }

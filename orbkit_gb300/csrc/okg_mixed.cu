@@ -61,6 +61,7 @@ struct Params {
     long long ld;
     int* status;           // device status word: 1 = timeout
     long long ntiles;
+    int brick, nby, nbz;   // tiling (see tiling())
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -209,7 +210,7 @@ struct MolDesc {
     BasisDev B;
     Grid g;
     const uint4* bpack;  // [npass][nmchunk][3][npad x 128 B], pre-swizzled
-    const double* occ;   // [npass * npad], zero padded
+    const double* occ;   // [npass * npad] occupations, then [npass * npad] 2 x occupations (zero padded)
     double* rho;
     double* grad;        // 3 x ld
     long long ld;
@@ -217,8 +218,14 @@ struct MolDesc {
     long long ntiles;
     int npass, npad;
     int want_grad;
-    int pad_;
+    int brick;           // regular grid covered by 4 x 4 x 8 bricks (else runs of 128 flattened points)
+    int nby, nbz;        // bricks along y and z
 };
+
+// Screening: a primitive is skipped for a tile when alpha log2(e) d^2 > SCREEN_LOG2,
+// d = distance from its atom to the tile's bounding box, i.e. its exponential is
+// below 2^-64 (5e-20) at every point of the tile.
+constexpr float SCREEN_LOG2 = 64.0f;
 
 // Shared-memory pieces of the CTA used by every tile.
 struct CtaState {
@@ -228,10 +235,59 @@ struct CtaState {
     uint32_t bar_a;
     uint32_t tmem;
     int* abort_flag;
+    float* bbox;                 // lo x,y,z, hi x,y,z of the current tile
+    float* bbox_part;            // 4 warps x 6
+    int* nkeep;                  // per shell of the current chunk: primitives kept
+    unsigned long long* kmask;   // columns of the current chunk whose shell is kept
 };
 
-// The whole computation of one 128-point tile of one molecule: per MO pass and
-// chunk, B copy + A generation + 96 MMAs, then the FP64 epilogue and the stores.
+// FP64 <-> FP32 without the FP64 pipe: rounding double -> float and exact
+// float -> double through integer operations on the IEEE bit patterns.
+__device__ __forceinline__ float dbl_to_flt_rn(double d)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const unsigned long long mag = u & 0x7FFFFFFFFFFFFFFFull;
+    if (mag < 0x3810000000000000ull) return 0.0f;  // |d| < 2^-126
+    u += 0x10000000ull;                           // round to nearest at the float's last bit
+    const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+    const unsigned e = (hi >> 20) & 0x7FF;
+    return __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+}
+
+__device__ __forceinline__ double flt_to_dbl(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFF;
+    if (e == 0) return 0.0;  // zero (denormals flushed)
+    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xFFFFFu)), (int)(u << 29));
+}
+
+// Point of row r of a tile.
+__device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int r, long long& p)
+{
+    if (D.brick) {
+        const long long bi = tile / ((long long)D.nby * D.nbz);
+        const int rem = (int)(tile - bi * (long long)D.nby * D.nbz);
+        const int bj = rem / D.nbz, bk = rem - bj * D.nbz;
+        const int i = (int)bi * 4 + (r >> 5), j = bj * 4 + ((r >> 3) & 3), k = bk * 8 + (r & 7);
+        if (i >= D.g.nx || j >= D.g.ny || k >= D.g.nz) {
+            p = 0;
+            return false;
+        }
+        p = ((long long)i * D.g.ny + j) * D.g.nz + k;
+        return true;
+    }
+    p = tile * M + r;
+    if (p >= D.g.npts) {
+        p = D.g.npts - 1;
+        return false;
+    }
+    return true;
+}
+
+// The whole computation of one 128-point tile of one molecule: bounding box, then
+// per MO pass and chunk: screening, B copy (screened columns zeroed), A generation
+// for kept shells, 96 MMAs; the FP64 epilogue; the stores.
 __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, const CtaState& S, uint32_t& phase,
                                            int* status)
 {
@@ -239,49 +295,125 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
     const int warp = tid >> 5;
     const int lane = tid & 31;
     const int prow = tid & (M - 1);  // point row of this thread in the tile
-    const int half = tid >> 7;       // generation: shells alternate between the two halves
+    const int half = tid >> 7;       // generation: atoms of a chunk alternate between the two halves
     const BasisDev& B = D.B;
     const int npad = D.npad;
     const uint32_t idesc = idesc_bf16(M, npad);
-    const int bbytes = 3 * npad * 128;
+    const int bunits = 3 * npad * 8;  // 16-byte units of one B block
     unsigned char* A_s = S.A_s;
     unsigned char* B_s = S.B_s;
     double* red = S.red;
 
-    const long long p = tile * M + prow;
-    const bool valid = p < D.g.npts;
+    long long p;
+    const bool valid = tile_point(D, tile, prow, p);
     double x, y, z;
-    grid_point(D.g, valid ? p : D.g.npts - 1, x, y, z);
+    grid_point(D.g, p, x, y, z);
+
+    // bounding box of the tile's valid points (rows 0..127 = warps 0..3)
+    {
+        float v[6];
+        v[0] = valid ? dbl_to_flt_rn(x) : 3.0e38f;
+        v[1] = valid ? dbl_to_flt_rn(y) : 3.0e38f;
+        v[2] = valid ? dbl_to_flt_rn(z) : 3.0e38f;
+        v[3] = valid ? dbl_to_flt_rn(x) : -3.0e38f;
+        v[4] = valid ? dbl_to_flt_rn(y) : -3.0e38f;
+        v[5] = valid ? dbl_to_flt_rn(z) : -3.0e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[c] = fminf(v[c], __shfl_xor_sync(0xffffffffu, v[c], o));
+#pragma unroll
+            for (int c = 3; c < 6; ++c) v[c] = fmaxf(v[c], __shfl_xor_sync(0xffffffffu, v[c], o));
+        }
+        if (warp < 4 && lane == 0)
+            for (int c = 0; c < 6; ++c) S.bbox_part[warp * 6 + c] = v[c];
+        __syncthreads();
+        if (tid < 6) {
+            float a = S.bbox_part[tid];
+            for (int w = 1; w < 4; ++w)
+                a = tid < 3 ? fminf(a, S.bbox_part[w * 6 + tid]) : fmaxf(a, S.bbox_part[w * 6 + tid]);
+            S.bbox[tid] = a;
+        }
+    }
     double rho_acc = 0.0, gx_acc = 0.0, gy_acc = 0.0, gz_acc = 0.0;
 
     for (int pass = 0; pass < D.npass; ++pass) {
+        bool pending = false;  // MMAs committed and not yet waited for
+        bool issued = false;   // some chunk of this pass reached the tensor core
         for (int c = 0; c < B.nmchunk; ++c) {
-            if (c > 0) {  // previous chunk's MMAs must be done before A/B are overwritten
+            const int4 ck = B.mchunks[c];
+            const int ns = ck.y - ck.x;
+            __syncthreads();  // bbox ready / previous chunk's screening data no longer read
+            if (tid == 0) *S.kmask = 0ull;
+            __syncthreads();
+            if (tid < ns) {
+                const Shell sh = B.shells[ck.x + tid];
+                const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
+                            az = (float)B.atoms[4 * sh.atom + 2];
+                const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
+                const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
+                const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                int nk = 0;
+                while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+                S.nkeep[tid] = nk;
+                if (nk > 0) {
+                    const int ncol = ncanon(sh.L);
+                    atomicOr(S.kmask, (((ncol == 64) ? ~0ull : ((1ull << ncol) - 1ull))) << sh.mcol);
+                }
+            }
+            __syncthreads();
+            const unsigned long long km = *S.kmask;
+            if (km == 0ull) continue;  // nothing of this chunk reaches the tile
+            if (pending) {             // previous chunk's MMAs must be done before A/B are overwritten
                 if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
                 phase ^= 1;
+                pending = false;
             }
-            // B block of this (pass, chunk)
-            const uint4* src = D.bpack + ((long long)pass * B.nmchunk + c) * (bbytes / 16);
-            for (int i = tid; i < bbytes / 16; i += NT) ((uint4*)B_s)[i] = src[i];
-            // A: AO values of this chunk's shells for this thread's point
-            const int4 ck = B.mchunks[c];
-            int last_atom = -1;
-            double X = 0, Y = 0, Z = 0, rr = 0;
-            float Xf = 0, Yf = 0, Zf = 0;
-            for (int s = ck.x + half; s < ck.y; s += 2) {
-                const Shell sh = B.shells[s];
-                if (sh.atom != last_atom) {
-                    X = x - B.atoms[4 * sh.atom];
-                    Y = y - B.atoms[4 * sh.atom + 1];
-                    Z = z - B.atoms[4 * sh.atom + 2];
-                    rr = X * X + Y * Y + Z * Z;
-                    Xf = (float)X;
-                    Yf = (float)Y;
-                    Zf = (float)Z;
-                    last_atom = sh.atom;
+            // B block of this (pass, chunk); columns of screened shells are zeroed
+            const uint4* src = D.bpack + ((long long)pass * B.nmchunk + c) * bunits;
+            for (int i = tid; i < bunits; i += NT) {
+                uint4 v = src[i];
+                const int n = (i >> 3) % npad;
+                const int lc = (i & 7) ^ (n & 7);  // logical 8-column group of this 16-byte unit
+                const unsigned m8 = (unsigned)(km >> (8 * lc)) & 0xFFu;
+                if (m8 != 0xFFu) {
+                    unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const unsigned keep = ((m8 >> (2 * q)) & 1u ? 0x0000FFFFu : 0u) |
+                                              ((m8 >> (2 * q + 1)) & 1u ? 0xFFFF0000u : 0u);
+                        w[q] &= keep;
+                    }
+                    v = make_uint4(w[0], w[1], w[2], w[3]);
                 }
+                ((uint4*)B_s)[i] = v;
+            }
+            // A: AO values of this chunk's kept shells for this thread's point; atoms
+            // (runs of shells on one atom) alternate between the two halves
+            int last_atom = -1, group = -1;
+            double rr = 0;
+            float Xf = 0, Yf = 0, Zf = 0;
+            for (int si = 0; si < ns; ++si) {
+                const Shell sh = B.shells[ck.x + si];
+                if (sh.atom != last_atom) {
+                    ++group;
+                    last_atom = sh.atom;
+                    if ((group & 1) == half) {
+                        const double X = x - B.atoms[4 * sh.atom];
+                        const double Y = y - B.atoms[4 * sh.atom + 1];
+                        const double Z = z - B.atoms[4 * sh.atom + 2];
+                        rr = X * X + Y * Y + Z * Z;
+                        Xf = dbl_to_flt_rn(X);
+                        Yf = dbl_to_flt_rn(Y);
+                        Zf = dbl_to_flt_rn(Z);
+                    }
+                }
+                if ((group & 1) != half) continue;
+                const int nk = S.nkeep[si];
+                if (nk == 0) continue;
                 float R0 = 0.f, R1 = 0.f;
-                for (int q = 0; q < sh.nprim; ++q) {
+                for (int q = 0; q < nk; ++q) {
                     const PrimMx pm = B.prim_mx[sh.prim0 + q];
                     const float e = exp2_neg(pm.a2 * rr);
                     R0 = fmaf(pm.w, e, R0);
@@ -305,6 +437,7 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                 tc_fence_after();
                 const uint32_t a0 = smem_u32(A_s), b0 = smem_u32(B_s);
                 const int bpart = npad * 128;
+                const uint32_t first = issued ? 0u : 1u;
 #pragma unroll 1
                 for (int ch = 0; ch < 4; ++ch) {
 #pragma unroll
@@ -319,13 +452,13 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                             uint32_t col, acc;
                             if (ch == 0 && t == 0) {         // leading product -> accumulator k
                                 col = k;
-                                acc = c > 0;
+                                acc = !first;
                             } else if (ch == 0) {            // value corrections -> accumulator 4
                                 col = 4;
-                                acc = (c > 0 || k > 0 || t > 1);
+                                acc = !first || k > 0 || t > 1;
                             } else {                         // gradient channel ch -> accumulator 4 + ch
                                 col = 4 + ch;
-                                acc = (c > 0 || k > 0 || t > 0);
+                                acc = !first || k > 0 || t > 0;
                             }
                             mma_bf16(S.tmem + col * npad, ad, bd, idesc, acc);
                         }
@@ -335,7 +468,10 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             } else if (tid == 0) {
                 asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(S.bar_a) : "memory");
             }
+            pending = true;
+            issued = true;
         }
+        if (!issued) continue;  // no AO of any chunk reaches this tile: this pass contributes zero
         // accumulators of this pass complete
         if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
         phase ^= 1;
@@ -345,6 +481,8 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             const int q = warp & 3, h = warp >> 2;
             const int nh = npad / 2;
             const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
+            const double* occ = D.occ + pass * npad;
+            const double* occ2 = D.occ + (D.npass + pass) * npad;
             double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
             for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
                 float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
@@ -361,12 +499,12 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                 for (int i = 0; i < 8; ++i) v0[i] = ((v0[i] + h1[i]) + (h2[i] + h3[i])) + lo[i];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const double o = __ldg(D.occ + pass * npad + m0 + i);
-                    racc = fma(o, (double)(v0[i] * v0[i]), racc);
-                    const double o2 = 2.0 * o;
-                    ga = fma(o2, (double)(v0[i] * v1[i]), ga);
-                    gb = fma(o2, (double)(v0[i] * v2[i]), gb);
-                    gc = fma(o2, (double)(v0[i] * v3[i]), gc);
+                    const double o = __ldg(occ + m0 + i);
+                    const double o2 = __ldg(occ2 + m0 + i);
+                    racc = fma(o, flt_to_dbl(v0[i] * v0[i]), racc);
+                    ga = fma(o2, flt_to_dbl(v0[i] * v1[i]), ga);
+                    gb = fma(o2, flt_to_dbl(v0[i] * v2[i]), gb);
+                    gc = fma(o2, flt_to_dbl(v0[i] * v3[i]), gc);
                 }
             }
             const int pt = 32 * q + lane;
@@ -379,7 +517,7 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             tc_fence_before();
             __syncthreads();
             if (h == 0) {
-                // warp w < 4, lane l: point 32 w + l == tid of this tile
+                // warp w < 4, lane l: point row 32 w + l == tid of this tile
                 rho_acc += racc + red[pt];
                 gx_acc += ga + red[M + pt];
                 gy_acc += gb + red[2 * M + pt];
@@ -399,9 +537,9 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
     }
 }
 
-// CTA set-up shared by the kernels: shared-memory carve-up, A zeroed (padding
-// columns must hold finite values), mbarrier, TMEM allocation (all 512 columns
-// when `cols` is 512).
+// CTA set-up shared by the kernels: shared-memory carve-up, A zeroed (columns of
+// screened shells keep stale but finite values, multiplied by zeroed B columns),
+// mbarrier, TMEM allocation.
 __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_cols)
 {
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -409,9 +547,13 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
     S.A_s = smem;
     S.B_s = smem + A_BYTES;
     S.red = (double*)(S.B_s + 3 * NMAX * 128);
-    uint64_t* bar = (uint64_t*)(S.red + 4 * M);
+    S.kmask = (unsigned long long*)(S.red + 4 * M);
+    uint64_t* bar = (uint64_t*)(S.kmask + 1);
     uint32_t* tmem_slot = (uint32_t*)(bar + 1);
     S.abort_flag = (int*)(tmem_slot + 1);
+    S.bbox = (float*)(S.abort_flag + 1);
+    S.bbox_part = S.bbox + 6;
+    S.nkeep = (int*)(S.bbox_part + 24);
     S.bar_a = smem_u32(bar);
     for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
@@ -432,6 +574,9 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
     return S;
 }
 
+// bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
+constexpr size_t SMEM_BYTES = 1024 + A_BYTES + 3 * NMAX * 128 + 4 * M * 8 + 8 + 8 + 8 + 4 * 6 + 4 * 24 + 4 * 64 + 64;
+
 __device__ __forceinline__ void cta_teardown(const CtaState& S, uint32_t tm_cols)
 {
     tc_fence_before();
@@ -444,6 +589,22 @@ __host__ __device__ inline uint32_t tmem_cols_for(int npad)
 {
     const int n = 8 * npad;
     return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
+}
+
+// Tiles of a grid: 4 x 4 x 8 bricks when the call covers a whole regular grid,
+// else runs of 128 flattened points.
+inline void tiling(const Grid& g, MolDesc& D)
+{
+    D.brick = g.regular && g.offset == 0 && g.npts == (long long)g.nx * g.ny * g.nz;
+    if (D.brick) {
+        const long long nbx = (g.nx + 3) / 4;
+        D.nby = (g.ny + 3) / 4;
+        D.nbz = (g.nz + 7) / 8;
+        D.ntiles = nbx * D.nby * D.nbz;
+    } else {
+        D.nby = D.nbz = 0;
+        D.ntiles = (g.npts + M - 1) / M;
+    }
 }
 
 extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
@@ -462,10 +623,13 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
     D.grad = P.grad;
     D.ld = P.ld;
     D.tile0 = 0;
-    D.ntiles = P.ntiles;
     D.npass = P.npass;
     D.npad = P.npad;
     D.want_grad = P.want_grad;
+    D.brick = P.brick;
+    D.nby = P.nby;
+    D.nbz = P.nbz;
+    D.ntiles = P.ntiles;
     uint32_t phase = 0;
     for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
         mixed_tile(D, tile, S, phase, P.status);
@@ -554,10 +718,15 @@ __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, 
     }
 }
 
+// out[0 .. total): occupations (zero padded); out[total .. 2 total): twice them.
 __global__ void pack_occ_kernel(const double* __restrict__ occ, int nmo, int total, double* __restrict__ out)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < total) out[i] = i < nmo ? occ[i] : 0.0;
+    if (i < total) {
+        const double o = i < nmo ? occ[i] : 0.0;
+        out[i] = o;
+        out[total + i] = 2.0 * o;
+    }
 }
 
 }  // namespace mx
@@ -605,7 +774,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->npad = (per + 15) / 16 * 16;
     p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * 128;
     const size_t occ_off = (p->bpack_bytes + 255) & ~(size_t)255;
-    const size_t st_off = occ_off + (((size_t)p->npass * p->npad * 8 + 255) & ~(size_t)255);
+    const size_t st_off = occ_off + (((size_t)2 * p->npass * p->npad * 8 + 255) & ~(size_t)255);
     cudaError_t e = cudaMalloc(&p->block, st_off + 256);
     if (e != cudaSuccess) {
         free(p);
@@ -616,7 +785,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->status = (int*)((char*)p->block + st_off);
     cudaMemset(p->status, 0, sizeof(int));
     p->sm_count = sms;
-    p->smem = 1024 + mx::A_BYTES + 3 * mx::NMAX * 128 + 4 * mx::M * 8 + 64;
+    p->smem = mx::SMEM_BYTES;
     e = cudaFuncSetAttribute(mx::rho_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
     if (e != cudaSuccess) {
         cudaFree(p->block);
@@ -679,7 +848,12 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     P.grad = d_grad;
     P.ld = ld;
     P.status = p->status;
-    P.ntiles = (g.npts + mx::M - 1) / mx::M;
+    mx::MolDesc T;
+    mx::tiling(g, T);
+    P.ntiles = T.ntiles;
+    P.brick = T.brick;
+    P.nby = T.nby;
+    P.nbz = T.nbz;
     const long long grid = P.ntiles < p->sm_count ? P.ntiles : p->sm_count;
     mx::rho_mixed_kernel<<<(unsigned)grid, mx::NT, p->smem, (cudaStream_t)stream>>>(P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
@@ -732,12 +906,11 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
         D.rho = d_rho[m];
         D.grad = want_grad ? d_grad[m] : nullptr;
         D.ld = ld[m];
-        D.ntiles = (gr->npts + mx::M - 1) / mx::M;
+        mx::tiling(D.g, D);
         D.tile0 = tile0;
         D.npass = p->npass;
         D.npad = p->npad;
         D.want_grad = want_grad;
-        D.pad_ = 0;
         tile0 += D.ntiles;
         sms = p->sm_count;
     }
@@ -761,7 +934,7 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
     b->sm_count = sms > 0 ? sms : 1;
     b->grab = 1;
     b->ctas = b->sm_count;
-    b->smem = 1024 + mx::A_BYTES + 3 * mx::NMAX * 128 + 4 * mx::M * 8 + 64;
+    b->smem = mx::SMEM_BYTES;
     e = cudaFuncSetAttribute(mx::rho_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
     if (e != cudaSuccess) {
         cudaFree(b->block);
@@ -881,7 +1054,7 @@ struct NoallocDevice {
 static NoallocDevice g_noalloc_dev[64];
 static std::mutex g_noalloc_mu;
 
-static size_t noalloc_smem() { return 1024 + A_BYTES + 3 * NMAX * 128 + 4 * M * 8 + 64; }
+static size_t noalloc_smem() { return SMEM_BYTES; }
 }  // namespace mx
 }  // namespace okg
 
@@ -914,7 +1087,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     const int npad = (per + 15) / 16 * 16;
     const size_t bpack_bytes = (size_t)npass * b->dev.nmchunk * 3 * npad * 128;
     const size_t occ_off = (bpack_bytes + 255) & ~(size_t)255;
-    const size_t st_off = occ_off + (((size_t)npass * npad * 8 + 255) & ~(size_t)255);
+    const size_t st_off = occ_off + (((size_t)2 * npass * npad * 8 + 255) & ~(size_t)255);
     if (st_off + 256 > NOALLOC_SCRATCH_BYTES)
         return set_error(OKG_ERR_UNSUPPORTED,
                          "okg_rho_mixed_noalloc: this basis and MO count need more than the 2 MiB of static "
@@ -965,7 +1138,12 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     P.grad = d_grad;
     P.ld = ld;
     P.status = status;
-    P.ntiles = (g.npts + M - 1) / M;
+    MolDesc T;
+    tiling(g, T);
+    P.ntiles = T.ntiles;
+    P.brick = T.brick;
+    P.nby = T.nby;
+    P.nbz = T.nbz;
     const long long grid = P.ntiles < nd->sm_count ? P.ntiles : nd->sm_count;
     rho_mixed_kernel<<<(unsigned)grid, NT, noalloc_smem(), st>>>(P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed_noalloc launch");
