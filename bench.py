@@ -379,6 +379,124 @@ def run_profile(args):
     print("profile run done: %d points" % npts)
 
 
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _time_ms(fn, steps, warmup, flush=None):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        if flush is not None:
+            flush.fill_(1)
+        e0, e1 = _events()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    return tot / steps
+
+
+def run_workload(args):
+    """Other workload shapes (one JSON line each; the default run is the mid workload)."""
+    import torch
+    from orbkit_gb300 import _lib, mixed, synthetic
+    from orbkit_gb300.core import _DeviceGrid
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    L = _lib.load()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    name = args.workload
+    out = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic", "dtype": "bf16"}
+    if name in ("small", "large"):
+        w = synthetic.small() if name == "small" else synthetic.large()
+        qc = w["qc"]
+        gx, gy, gz = w["grid"]
+        npts = len(gx) * len(gy) * len(gz)
+        ev = mixed.MixedEvaluator(qc, device=dev)
+        g = _DeviceGrid(gx, gy, gz, False, dev)
+        rho = torch.empty(npts, dtype=torch.float64, device=dev)
+        grad = torch.empty((3, npts), dtype=torch.float64, device=dev)
+        ms = _time_ms(lambda: ev.evaluate_device(g, rho, grad), args.steps, args.warmup, flush)
+        ev.check()
+        # FP64 path: whole grid (small) or a contiguous slice of 2^18 points (large)
+        n64 = npts if name == "small" else 1 << 18
+        gd, keep = g.slice(npts // 2, npts // 2 + n64) if n64 < npts else g.slice(0, npts)
+        r64 = torch.empty(n64, dtype=torch.float64, device=dev)
+        g64 = torch.empty((3, n64), dtype=torch.float64, device=dev)
+        p = ev.plan
+        fp64_ms = _time_ms(lambda: _lib.check(L.okg_rho(ev.basis.handle, gd, p.nmo, _lib.ptr(p.C), _lib.ptr(p.occ),
+                                                        3, _lib.int_array([1, 2, 3]), 0, _lib.ptr(r64),
+                                                        _lib.ptr(g64), n64, None, _lib.stream_handle())), 1, 1)
+        s0 = npts // 2 if n64 < npts else 0
+        err = mixed.error_report(rho[s0:s0 + n64].cpu().numpy(), grad[:, s0:s0 + n64].cpu().numpy(),
+                                 r64.cpu().numpy(), g64.cpu().numpy())
+        out.update({"value": npts / (ms * 1e-3), "ms_per_step": ms,
+                    "config": {"workload": name, "npts": npts, "nao": ev.basis.nao, "ncart": ev.basis.ncart,
+                               "nmo": p.nmo, "spherical": ev.basis.spherical, "path": "mixed",
+                               "fp64_path": {"value": n64 / (fp64_ms * 1e-3), "points_timed": n64},
+                               "mixed_over_fp64": (n64 / fp64_ms) and (npts / ms) / (n64 / fp64_ms),
+                               "max_rel_err": dict(err, against="FP64 GPU path on the %d points it timed" % n64)}})
+        if not args.no_cpu_baseline:
+            rate, cores, n, dt = cpu_rate(qc, gx, gy, gz, target_s=8.0)
+            out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                   "sample": "%d random grid points, %.1f s" % (n, dt)}
+    elif name == "grad":
+        from orbkit_gb300.adjoint import DensityModel, density_fit_loss
+        w = synthetic.grad()
+        qc = w["qc"]
+        x, y, z = w["grid"]
+        prim = qc.ao_spec.get_prim_coeffs()
+        res = {}
+        for prec in ("fp64", "fp32"):
+            model = DensityModel(qc, x, y, z, False, prec)
+            t = w["target"]
+            with torch.no_grad():
+                rt, gt = model(torch.tensor(t["coeffs"], device=dev), torch.tensor(t["alpha"], device=dev),
+                               torch.tensor(prim[:, 1], device=dev), torch.tensor(t["geo"], device=dev))
+                rt, gt = rt.clone(), gt.clone()
+            wts = torch.tensor(numpy.random.default_rng(w["weight_seed"]).uniform(1e-12, 1, model.npts), device=dev)
+            C = torch.tensor(qc.mo_spec.get_coeffs(), device=dev, requires_grad=True)
+            a = torch.tensor(prim[:, 0], device=dev, requires_grad=True)
+            c = torch.tensor(prim[:, 1], device=dev, requires_grad=True)
+            gg = torch.tensor(numpy.asarray(qc.geo_spec), device=dev, requires_grad=True)
+
+            def step():
+                for q in (C, a, c, gg):
+                    q.grad = None
+                density_fit_loss(*model(C, a, c, gg), rt, gt, wts).backward()
+            res[prec] = (_time_ms(step, args.steps, args.warmup, flush), model.npts,
+                         [q.grad.detach().clone() for q in (C, a, c, gg)])
+        rel = [float((g32 - g64).abs().max() / g64.abs().max()) for g32, g64 in zip(res["fp32"][2], res["fp64"][2])]
+        npts = res["fp64"][1]
+        out.update({"metric": "grid points/s for loss + gradient (dL/dC, dL/dalpha, dL/dc, dL/dR), FP32 vs FP64",
+                    "value": npts / (res["fp32"][0] * 1e-3), "ms_per_step": res["fp32"][0],
+                    "config": {"workload": "grad: 12 atoms, 128^3 grid, density-fitting loss, forward + adjoint",
+                               "npts": npts, "fp64": {"value": npts / (res["fp64"][0] * 1e-3),
+                                                      "ms_per_step": res["fp64"][0]},
+                               "fp32_vs_fp64_gradient_rel_err": dict(zip(["C", "alpha", "c", "R"], rel))}})
+    elif name == "batch":
+        from orbkit_gb300.batch import BatchEvaluator
+        d = synthetic.batch()
+        mols = [(m["qc"], m["points"]) for m in d["molecules"]]
+        npts = sum(pp.shape[1] for _, pp in mols)
+        ev = BatchEvaluator(mols, cusp_radius=0.0, tune=True)
+        graph = ev.capture()
+        ms = _time_ms(graph.replay, args.steps, args.warmup)
+        ev.check()
+        out.update({"value": npts / (ms * 1e-3), "ms_per_step": ms,
+                    "config": {"workload": "batch: 256 molecules, 3-60 atoms, atom-centred point sets",
+                               "npts": npts, "molecules": len(mols), "tiles": ev.tiles(), "schedule": ev.schedule,
+                               "launch": "CUDA graph replay of one persistent kernel", "cusp_radius": 0.0}})
+    print(json.dumps(out))
+
+
 def ctypes_fp64_rate(L):
     import ctypes
     v = ctypes.c_double(0)
@@ -396,9 +514,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--profile", action="store_true", help="minimal launch sequence for ncu captures")
+    ap.add_argument("--workload", default="mid", choices=["mid", "small", "grad", "batch", "large"])
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.workload != "mid" and args.impl == "ours":
+        if args.warmup < 3:
+            args.warmup = 3
+        return run_workload(args)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -279,6 +279,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
             }
             if (s < nshell) {
                 shells[s].mcol = col;
+                shells[s].mchunk = (int)mchunks.size();
                 col += nk;
             }
         }

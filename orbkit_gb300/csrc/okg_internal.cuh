@@ -51,7 +51,7 @@ struct Shell {
     int nout;   // output rows (ncart or number of spherical functions)
     int sph0;   // first spherical row's index into sph_ptr (spherical bases)
     int mcol;   // mixed path: first column of this shell inside its chunk (canonical order)
-    int pad;
+    int mchunk; // mixed path: index of the chunk holding this shell
 };
 
 // Per-primitive data of the mixed path: alpha*log2(e) in FP64 (the exponent

@@ -62,6 +62,7 @@ struct Params {
     int* status;           // device status word: 1 = timeout
     long long ntiles;
     int brick, nby, nbz;   // tiling (see tiling())
+    unsigned long long* counter;  // tile counter, zero at launch (tiles are handed out dynamically)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -211,6 +212,7 @@ struct MolDesc {
     Grid g;
     const uint4* bpack;  // [npass][nmchunk][3][npad x 128 B], pre-swizzled
     const double* occ;   // [npass * npad] occupations, then [npass * npad] 2 x occupations (zero padded)
+    const float2* occf;  // the same 2 x npass x npad values as double-float (hi, lo) pairs
     double* rho;
     double* grad;        // 3 x ld
     long long ld;
@@ -237,9 +239,14 @@ struct CtaState {
     int* abort_flag;
     float* bbox;                 // lo x,y,z, hi x,y,z of the current tile
     float* bbox_part;            // 4 warps x 6
-    int* nkeep;                  // per shell of the current chunk: primitives kept
-    unsigned long long* kmask;   // columns of the current chunk whose shell is kept
+    unsigned char* nkeep;        // per shell: primitives kept for the current tile
+    unsigned long long* kmask;   // per chunk: columns whose shell is kept for the current tile
 };
+
+// Per-tile screening tables live in shared memory: at most MAX_SHELLS shells and
+// MAX_CHUNKS chunks per molecule on the mixed path.
+constexpr int MAX_SHELLS = 2048;
+constexpr int MAX_CHUNKS = 128;
 
 // FP64 <-> FP32 without the FP64 pipe: rounding double -> float and exact
 // float -> double through integer operations on the IEEE bit patterns.
@@ -260,6 +267,30 @@ __device__ __forceinline__ double flt_to_dbl(float f)
     const unsigned e = (u >> 23) & 0xFF;
     if (e == 0) return 0.0;  // zero (denormals flushed)
     return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xFFFFFu)), (int)(u << 29));
+}
+
+// Double-float (hi + lo, FP32) accumulation: two-sum of the high parts, low parts
+// collected separately (Dekker / Knuth); products exact through FMA.
+struct DF {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float2 t)
+    {
+        const float s = hi + t.x;
+        const float bb = s - hi;
+        const float err = (hi - (s - bb)) + (t.x - bb);
+        hi = s;
+        lo += err + t.y;
+    }
+};
+
+// (o.x + o.y) * (a * b) as a double-float (a * b exact: p + e with e = fma(a, b, -p))
+__device__ __forceinline__ float2 df_mul(float2 o, float a, float b)
+{
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float q = o.x * p;
+    const float r = fmaf(o.x, p, -q) + (o.x * e + o.y * p);
+    return make_float2(q, r);
 }
 
 // Point of row r of a tile.
@@ -335,6 +366,23 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             S.bbox[tid] = a;
         }
     }
+    // screening of every shell against the tile's bounding box, once per tile
+    for (int c = tid; c < B.nmchunk; c += NT) S.kmask[c] = 0ull;
+    __syncthreads();
+    for (int si = tid; si < B.nshell; si += NT) {
+        const Shell sh = B.shells[si];
+        const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
+                    az = (float)B.atoms[4 * sh.atom + 2];
+        const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
+        const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
+        const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        int nk = 0;
+        while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+        S.nkeep[si] = (unsigned char)nk;
+        if (nk > 0) atomicOr(S.kmask + sh.mchunk, ((1ull << ncanon(sh.L)) - 1ull) << sh.mcol);
+    }
+    __syncthreads();
     double rho_acc = 0.0, gx_acc = 0.0, gy_acc = 0.0, gz_acc = 0.0;
 
     for (int pass = 0; pass < D.npass; ++pass) {
@@ -343,27 +391,7 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
         for (int c = 0; c < B.nmchunk; ++c) {
             const int4 ck = B.mchunks[c];
             const int ns = ck.y - ck.x;
-            __syncthreads();  // bbox ready / previous chunk's screening data no longer read
-            if (tid == 0) *S.kmask = 0ull;
-            __syncthreads();
-            if (tid < ns) {
-                const Shell sh = B.shells[ck.x + tid];
-                const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
-                            az = (float)B.atoms[4 * sh.atom + 2];
-                const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
-                const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
-                const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                int nk = 0;
-                while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
-                S.nkeep[tid] = nk;
-                if (nk > 0) {
-                    const int ncol = ncanon(sh.L);
-                    atomicOr(S.kmask, (((ncol == 64) ? ~0ull : ((1ull << ncol) - 1ull))) << sh.mcol);
-                }
-            }
-            __syncthreads();
-            const unsigned long long km = *S.kmask;
+            const unsigned long long km = S.kmask[c];
             if (km == 0ull) continue;  // nothing of this chunk reaches the tile
             if (pending) {             // previous chunk's MMAs must be done before A/B are overwritten
                 if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
@@ -410,7 +438,7 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                     }
                 }
                 if ((group & 1) != half) continue;
-                const int nk = S.nkeep[si];
+                const int nk = S.nkeep[ck.x + si];
                 if (nk == 0) continue;
                 float R0 = 0.f, R1 = 0.f;
                 for (int q = 0; q < nk; ++q) {
@@ -435,8 +463,9 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             __syncthreads();
             if (tid == 0 && !*S.abort_flag) {
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(A_s), b0 = smem_u32(B_s);
-                const int bpart = npad * 128;
+                // descriptors differ only in the start-address field (bytes >> 4)
+                const uint64_t adesc = sdesc(smem_u32(A_s)), bdesc = sdesc(smem_u32(B_s));
+                const uint32_t bpart16 = (uint32_t)(npad * 128) >> 4;
                 const uint32_t first = issued ? 0u : 1u;
 #pragma unroll 1
                 for (int ch = 0; ch < 4; ++ch) {
@@ -447,8 +476,8 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                         const int pb[6] = {0, 1, 0, 2, 1, 0};
 #pragma unroll
                         for (int t = 0; t < 6; ++t) {
-                            const uint64_t ad = sdesc(a0 + (ch * 3 + pa[t]) * A_TILE + k * 32);
-                            const uint64_t bd = sdesc(b0 + pb[t] * bpart + k * 32);
+                            const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 32) >> 4);
+                            const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
                             uint32_t col, acc;
                             if (ch == 0 && t == 0) {         // leading product -> accumulator k
                                 col = k;
@@ -481,8 +510,8 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             const int q = warp & 3, h = warp >> 2;
             const int nh = npad / 2;
             const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
-            const double* occ = D.occ + pass * npad;
-            const double* occ2 = D.occ + (D.npass + pass) * npad;
+            const float2* occf = D.occf + pass * npad;
+            const float2* occ2f = D.occf + (D.npass + pass) * npad;
             double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
             for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
                 float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
@@ -497,15 +526,23 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                 tmem_wait_ld();
 #pragma unroll
                 for (int i = 0; i < 8; ++i) v0[i] = ((v0[i] + h1[i]) + (h2[i] + h3[i])) + lo[i];
+                // sum_i occ_i v0_i^2 and sum_i 2 occ_i v0_i vd_i over the 8 MOs in double-float
+                // FP32 arithmetic (exact products by FMA, two-sum accumulation, about 44
+                // bits), then add the group sums to the FP64 accumulators
+                DF sr, sa, sb, sc;
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const double o = __ldg(occ + m0 + i);
-                    const double o2 = __ldg(occ2 + m0 + i);
-                    racc = fma(o, flt_to_dbl(v0[i] * v0[i]), racc);
-                    ga = fma(o2, flt_to_dbl(v0[i] * v1[i]), ga);
-                    gb = fma(o2, flt_to_dbl(v0[i] * v2[i]), gb);
-                    gc = fma(o2, flt_to_dbl(v0[i] * v3[i]), gc);
+                    const float2 o = __ldg(occf + m0 + i);
+                    const float2 o2 = __ldg(occ2f + m0 + i);
+                    sr.add(df_mul(o, v0[i], v0[i]));
+                    sa.add(df_mul(o2, v0[i], v1[i]));
+                    sb.add(df_mul(o2, v0[i], v2[i]));
+                    sc.add(df_mul(o2, v0[i], v3[i]));
                 }
+                racc += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
+                ga += flt_to_dbl(sa.hi) + flt_to_dbl(sa.lo);
+                gb += flt_to_dbl(sb.hi) + flt_to_dbl(sb.lo);
+                gc += flt_to_dbl(sc.hi) + flt_to_dbl(sc.lo);
             }
             const int pt = 32 * q + lane;
             if (h == 1) {
@@ -548,12 +585,12 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
     S.B_s = smem + A_BYTES;
     S.red = (double*)(S.B_s + 3 * NMAX * 128);
     S.kmask = (unsigned long long*)(S.red + 4 * M);
-    uint64_t* bar = (uint64_t*)(S.kmask + 1);
+    uint64_t* bar = (uint64_t*)(S.kmask + MAX_CHUNKS);
     uint32_t* tmem_slot = (uint32_t*)(bar + 1);
     S.abort_flag = (int*)(tmem_slot + 1);
     S.bbox = (float*)(S.abort_flag + 1);
     S.bbox_part = S.bbox + 6;
-    S.nkeep = (int*)(S.bbox_part + 24);
+    S.nkeep = (unsigned char*)(S.bbox_part + 24);
     S.bar_a = smem_u32(bar);
     for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
@@ -575,7 +612,9 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
 }
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
-constexpr size_t SMEM_BYTES = 1024 + A_BYTES + 3 * NMAX * 128 + 4 * M * 8 + 8 + 8 + 8 + 4 * 6 + 4 * 24 + 4 * 64 + 64;
+constexpr size_t SMEM_BYTES =
+    1024 + A_BYTES + 3 * NMAX * 128 + 4 * M * 8 + 8 * MAX_CHUNKS + 8 + 8 + 4 * 6 + 4 * 24 + MAX_SHELLS + 64;
+static_assert(SMEM_BYTES <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 
 __device__ __forceinline__ void cta_teardown(const CtaState& S, uint32_t tm_cols)
 {
@@ -619,6 +658,7 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
     D.g = P.g;
     D.bpack = P.bpack;
     D.occ = P.occ;
+    D.occf = (const float2*)(P.occ + 2 * P.npass * P.npad);
     D.rho = P.rho;
     D.grad = P.grad;
     D.ld = P.ld;
@@ -631,9 +671,14 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
     D.nbz = P.nbz;
     D.ntiles = P.ntiles;
     uint32_t phase = 0;
-    for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+    __shared__ long long next_tile;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) next_tile = (long long)atomicAdd(P.counter, 1ull);
+        __syncthreads();
+        const long long tile = next_tile;
+        if (tile >= P.ntiles || *S.abort_flag) break;
         mixed_tile(D, tile, S, phase, P.status);
-        if (*S.abort_flag) break;
     }
     cta_teardown(S, tm_cols);
 }
@@ -718,7 +763,8 @@ __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, 
     }
 }
 
-// out[0 .. total): occupations (zero padded); out[total .. 2 total): twice them.
+// out[0 .. total): occupations (zero padded); out[total .. 2 total): twice them;
+// then the same 2 total values as double-float (hi, lo) pairs.
 __global__ void pack_occ_kernel(const double* __restrict__ occ, int nmo, int total, double* __restrict__ out)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -726,6 +772,10 @@ __global__ void pack_occ_kernel(const double* __restrict__ occ, int nmo, int tot
         const double o = i < nmo ? occ[i] : 0.0;
         out[i] = o;
         out[total + i] = 2.0 * o;
+        float2* f = (float2*)(out + 2 * total);
+        const float oh = (float)o, o2h = (float)(2.0 * o);
+        f[i] = make_float2(oh, (float)(o - (double)oh));
+        f[total + i] = make_float2(o2h, (float)(2.0 * o - (double)o2h));
     }
 }
 
@@ -765,6 +815,8 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (major != 10 || minor != 3) return set_error(OKG_ERR_DEVICE, "okg_mixed_plan_create: needs an sm_103 GPU");
+    if (b->dev.nshell > mx::MAX_SHELLS || b->dev.nmchunk > mx::MAX_CHUNKS)
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: more than 2048 shells or 128 column chunks");
     okg_mixed_plan* p = (okg_mixed_plan*)calloc(1, sizeof(okg_mixed_plan));
     if (!p) return set_error(OKG_ERR_ALLOC, "okg_mixed_plan_create: host allocation");
     p->basis = b;
@@ -774,7 +826,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->npad = (per + 15) / 16 * 16;
     p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * 128;
     const size_t occ_off = (p->bpack_bytes + 255) & ~(size_t)255;
-    const size_t st_off = occ_off + (((size_t)2 * p->npass * p->npad * 8 + 255) & ~(size_t)255);
+    const size_t st_off = occ_off + (((size_t)4 * p->npass * p->npad * 8 + 255) & ~(size_t)255);
     cudaError_t e = cudaMalloc(&p->block, st_off + 256);
     if (e != cudaSuccess) {
         free(p);
@@ -848,6 +900,11 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     P.grad = d_grad;
     P.ld = ld;
     P.status = p->status;
+    P.counter = (unsigned long long*)((char*)p->status + 64);
+    {
+        cudaError_t e0 = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), (cudaStream_t)stream);
+        if (e0 != cudaSuccess) return cuda_status(e0, "okg_rho_mixed: counter reset");
+    }
     mx::MolDesc T;
     mx::tiling(g, T);
     P.ntiles = T.ntiles;
@@ -903,6 +960,7 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
         D.g.regular = gr->regular;
         D.bpack = (const uint4*)p->bpack;
         D.occ = p->occ;
+        D.occf = (const float2*)(p->occ + 2 * p->npass * p->npad);
         D.rho = d_rho[m];
         D.grad = want_grad ? d_grad[m] : nullptr;
         D.ld = ld[m];
@@ -1087,7 +1145,9 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     const int npad = (per + 15) / 16 * 16;
     const size_t bpack_bytes = (size_t)npass * b->dev.nmchunk * 3 * npad * 128;
     const size_t occ_off = (bpack_bytes + 255) & ~(size_t)255;
-    const size_t st_off = occ_off + (((size_t)2 * npass * npad * 8 + 255) & ~(size_t)255);
+    const size_t st_off = occ_off + (((size_t)4 * npass * npad * 8 + 255) & ~(size_t)255);
+    if (b->dev.nshell > MAX_SHELLS || b->dev.nmchunk > MAX_CHUNKS)
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: more than 2048 shells or 128 column chunks");
     if (st_off + 256 > NOALLOC_SCRATCH_BYTES)
         return set_error(OKG_ERR_UNSUPPORTED,
                          "okg_rho_mixed_noalloc: this basis and MO count need more than the 2 MiB of static "
@@ -1138,6 +1198,9 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     P.grad = d_grad;
     P.ld = ld;
     P.status = status;
+    P.counter = (unsigned long long*)(nd->base + st_off + 64);
+    e = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: counter reset");
     MolDesc T;
     tiling(g, T);
     P.ntiles = T.ntiles;

@@ -132,17 +132,54 @@ class MixedEvaluator:
             _lib.check(p._L.okg_mixed_set_coeffs(p.handle, _lib.ptr(p.C), _lib.ptr(p.occ), _lib.stream_handle(stream)))
 
     def evaluate_device(self, g, rho=None, grad=None):
-        """Run on a _DeviceGrid; returns device tensors (rho, grad)."""
+        """Run on a _DeviceGrid; returns device tensors (rho, grad).  The FP64
+        recomputation of the cusp points runs on a side stream concurrently with
+        the mixed kernel and is scattered into the outputs afterwards."""
         import torch
         n = g.npts
         if rho is None:
             rho = torch.empty(n, dtype=torch.float64, device=self.device)
             grad = torch.empty((3, n), dtype=torch.float64, device=self.device)
         gd, keep = g.slice(0, n)
-        self.plan.rho(gd, rho, grad, n)
+        fix = None
         if self.cusp_radius and self.cusp_radius > 0:
-            fix_cusp(self.plan, self.geo, g, rho, grad, self.cusp_radius)
+            fix = self._cusp_launch(g)
+        self.plan.rho(gd, rho, grad, n)
+        if fix is not None:
+            idx, r, dr, ev = fix
+            torch.cuda.current_stream().wait_event(ev)
+            rho.index_copy_(0, idx, r)
+            grad.index_copy_(1, idx, dr)
         return rho, grad
+
+    def _cusp_launch(self, g):
+        import torch
+        key = (tuple((v.__array_interface__["data"][0], v.shape) for v in g.host), g.regular, self.cusp_radius,
+               self.geo.tobytes())
+        if getattr(self, "_cusp_key", None) != key:
+            self._cusp_key = key
+            self._cusp = cusp_points(self.geo, g, self.cusp_radius, self.device)
+            self._side = torch.cuda.Stream(device=self.device)
+        idx, pts = self._cusp
+        m = len(idx)
+        if m == 0:
+            return None
+        main = torch.cuda.current_stream()
+        self._side.wait_stream(main)
+        with torch.cuda.stream(self._side):
+            r = torch.empty(m, dtype=torch.float64, device=self.device)
+            dr = torch.empty((3, m), dtype=torch.float64, device=self.device)
+            gd = _lib.OkgGrid(pts[0].data_ptr(), pts[1].data_ptr(), pts[2].data_ptr(), m, 0, 0, 0, 0, 0)
+            L = _lib.load()
+            p = self.plan
+            _lib.check(L.okg_rho(p.basis.handle, gd, p.nmo, _lib.ptr(p.C), _lib.ptr(p.occ), 3,
+                                 _lib.int_array([1, 2, 3]), 1, _lib.ptr(r), _lib.ptr(dr), m, None,
+                                 _lib.stream_handle(self._side)))
+            ev = torch.cuda.Event()
+            ev.record(self._side)
+        r.record_stream(main)
+        dr.record_stream(main)
+        return idx, r, dr, ev
 
     def evaluate(self, x, y, z, is_vector, out=None):
         """Host grid in, host (rho, grad) out.  `out` may hold preallocated (pinned)
@@ -176,6 +213,24 @@ def rho_grad(qc, x, y, z, is_vector, cusp_radius=CUSP_RADIUS, return_device=Fals
     out = ev.evaluate(x, y, z, is_vector)
     ev.check()
     return out
+
+
+def cusp_points(geo, g, radius, device):
+    """(flattened indices, (3, m) coordinates) of the grid points within `radius` of a nucleus."""
+    import torch
+    if g.regular:
+        idx = cusp_points_regular(geo, *g.host, radius)
+        gx, gy, gz = g.host
+        nyz = len(gy) * len(gz)
+        pts = numpy.stack([gx[idx // nyz], gy[(idx // len(gz)) % len(gy)], gz[idx % len(gz)]])
+        return torch.from_numpy(idx).to(device), torch.from_numpy(pts).to(device)
+    pts_all = torch.stack([torch.from_numpy(numpy.ascontiguousarray(v)).to(device) for v in g.host])
+    G = torch.as_tensor(numpy.asarray(geo, dtype=numpy.float64), device=device)
+    near = torch.zeros(pts_all.shape[1], dtype=torch.bool, device=device)
+    for a in range(G.shape[0]):
+        near |= ((pts_all - G[a][:, None]) ** 2).sum(0) <= radius * radius
+    it = torch.nonzero(near).flatten()
+    return it, pts_all[:, it].contiguous()
 
 
 def fix_cusp(plan, geo, g, rho, grad, radius):
