@@ -135,6 +135,9 @@ int okg_mixed_plan_create(const okg_basis* basis, int nmo, okg_mixed_plan** out)
  * autotuner -- fewer columns per pass, more passes. */
 int okg_mixed_plan_create_tiled(const okg_basis* basis, int nmo, int n_max, okg_mixed_plan** out);
 int okg_mixed_plan_destroy(okg_mixed_plan* plan);
+/* Threads per CTA of the plan's launches: 256, 384 or 512 (2, 3 or 4 threads share the
+ * AO generation of each of the tile's 128 points). */
+int okg_mixed_plan_set_threads(okg_mixed_plan* plan, int threads);
 /* Split C_eff (nmo x ncart, FP64, device) into the BF16 operand tiles; copy occ (nmo). */
 int okg_mixed_set_coeffs(okg_mixed_plan* plan, const double* d_coeff, const double* d_occ, okg_stream stream);
 /* d_rho[i]; d_grad[c * ld + i] for c = x, y, z when want_grad. */
@@ -152,13 +155,13 @@ int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
  * molecule; tiles of 128 points are numbered across molecules in the given order
  * and handed out to one CTA per SM through a device counter.  okg_batch_run is a
  * counter reset plus one kernel launch on `stream` and can be captured in a CUDA
- * graph.  okg_batch_set_schedule sets the tiles taken per counter increment and the
- * number of CTAs (the autotuner's knobs). */
+ * graph.  okg_batch_set_schedule sets the tiles taken per counter increment, the
+ * number of CTAs and the threads per CTA (the autotuner's knobs). */
 typedef struct okg_batch okg_batch;
 int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* grids, double* const* d_rho,
                      double* const* d_grad, const int64_t* ld, int want_grad, okg_batch** out);
 int okg_batch_destroy(okg_batch* batch);
-int okg_batch_set_schedule(okg_batch* batch, int tiles_per_grab, int ctas);
+int okg_batch_set_schedule(okg_batch* batch, int tiles_per_grab, int ctas, int threads);
 int okg_batch_tiles(const okg_batch* batch, long long* total_tiles);
 int okg_batch_run(okg_batch* batch, okg_stream stream);
 int okg_batch_status(okg_batch* batch, int* device_status);

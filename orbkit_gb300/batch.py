@@ -27,15 +27,16 @@ _SIGS = {
                                         ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "okg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
-    "okg_batch_set_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "okg_batch_set_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "okg_batch_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "okg_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "okg_batch_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
 }
 
 N_TILES = (32, 64)
-GRABS = (1, 2, 4)
+GRABS = (1, 4)
 ORDERS = ("given", "largest_first")
+THREADS = (256, 384, 512)
 
 
 def _L():
@@ -87,7 +88,7 @@ class BatchEvaluator:
         self._batch = None
         self._cusp = None
         if schedule is None:
-            schedule = self.autotune() if tune else {"n_max": 64, "grab": 1, "order": "given"}
+            schedule = self.autotune() if tune else {"n_max": 64, "grab": 1, "order": "given", "threads": 256}
         self.set_schedule(schedule)
 
     # ------------------------------------------------------------- schedule
@@ -126,7 +127,7 @@ class BatchEvaluator:
                                             ctypes.byref(h)))
         self._batch = h
         sms = __import__("torch").cuda.get_device_properties(self.device).multi_processor_count
-        _lib.check(self._L.okg_batch_set_schedule(h, sch["grab"], sms))
+        _lib.check(self._L.okg_batch_set_schedule(h, sch["grab"], sms, sch.get("threads", 256)))
         self.schedule = dict(sch)
 
     def tiles(self):
@@ -139,7 +140,8 @@ class BatchEvaluator:
         key = "batch-" + autotune.bucket(nmol=len(self.mols), pts=self.npts,
                                          nao=max(m["basis"].ncart for m in self.mols),
                                          nmo=max(len(m["occ"]) for m in self.mols))
-        cands = [{"n_max": n, "grab": g, "order": o} for n in N_TILES for g in GRABS for o in ORDERS]
+        cands = [{"n_max": n, "grab": g, "order": o, "threads": t}
+                 for n in N_TILES for g in GRABS for o in ORDERS for t in THREADS]
 
         def measure(c):
             self.set_schedule(c)

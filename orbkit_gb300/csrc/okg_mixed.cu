@@ -43,7 +43,7 @@ namespace mx {
 
 constexpr int M = 128;
 constexpr int KC = OKG_MKC;           // 64 BF16 = 128 bytes
-constexpr int NT = 256;               // 8 warps
+constexpr int NG_DEFAULT = 4;         // generation groups per point (threads = 128 x groups); 512 threads measured fastest on the mid workload
 constexpr int A_TILE = M * 128;       // bytes of one 128 x 64 BF16 sub-tile
 constexpr int A_BYTES = 12 * A_TILE;  // 4 channels x 3 parts
 constexpr int NMAX = 64;              // MO columns per pass
@@ -293,6 +293,18 @@ __device__ __forceinline__ float2 df_mul(float2 o, float a, float b)
     return make_float2(q, r);
 }
 
+// A Shell (12 ints, 16-byte aligned in the basis block) as three 16-byte loads.
+__device__ __forceinline__ Shell load_shell(const Shell* p)
+{
+    const int4* q = reinterpret_cast<const int4*>(p);
+    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    Shell s;
+    s.atom = a.x; s.L = a.y; s.nprim = a.z; s.prim0 = a.w;
+    s.cart0 = b.x; s.ncart = b.y; s.comp0 = b.z; s.out0 = b.w;
+    s.nout = c.x; s.sph0 = c.y; s.mcol = c.z; s.mchunk = c.w;
+    return s;
+}
+
 // Point of row r of a tile.
 __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int r, long long& p)
 {
@@ -319,21 +331,22 @@ __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int
 // The whole computation of one 128-point tile of one molecule: bounding box, then
 // per MO pass and chunk: screening, B copy (screened columns zeroed), A generation
 // for kept shells, 96 MMAs; the FP64 epilogue; the stores.
+template <int NG>
 __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, const CtaState& S, uint32_t& phase,
                                            int* status)
 {
+    constexpr int NTT = 128 * NG;
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
     const int lane = tid & 31;
     const int prow = tid & (M - 1);  // point row of this thread in the tile
-    const int half = tid >> 7;       // generation: atoms of a chunk alternate between the two halves
+    const int half = tid >> 7;       // generation group: atoms of a chunk go round-robin to the NG groups
     const BasisDev& B = D.B;
     const int npad = D.npad;
     const uint32_t idesc = idesc_bf16(M, npad);
     const int bunits = 3 * npad * 8;  // 16-byte units of one B block
     unsigned char* A_s = S.A_s;
     unsigned char* B_s = S.B_s;
-    double* red = S.red;
 
     long long p;
     const bool valid = tile_point(D, tile, prow, p);
@@ -367,10 +380,10 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
         }
     }
     // screening of every shell against the tile's bounding box, once per tile
-    for (int c = tid; c < B.nmchunk; c += NT) S.kmask[c] = 0ull;
+    for (int c = tid; c < B.nmchunk; c += NTT) S.kmask[c] = 0ull;
     __syncthreads();
-    for (int si = tid; si < B.nshell; si += NT) {
-        const Shell sh = B.shells[si];
+    for (int si = tid; si < B.nshell; si += NTT) {
+        const Shell sh = load_shell(B.shells + si);
         const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
                     az = (float)B.atoms[4 * sh.atom + 2];
         const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
@@ -400,7 +413,7 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             }
             // B block of this (pass, chunk); columns of screened shells are zeroed
             const uint4* src = D.bpack + ((long long)pass * B.nmchunk + c) * bunits;
-            for (int i = tid; i < bunits; i += NT) {
+            for (int i = tid; i < bunits; i += NTT) {
                 uint4 v = src[i];
                 const int n = (i >> 3) % npad;
                 const int lc = (i & 7) ^ (n & 7);  // logical 8-column group of this 16-byte unit
@@ -423,11 +436,11 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
             double rr = 0;
             float Xf = 0, Yf = 0, Zf = 0;
             for (int si = 0; si < ns; ++si) {
-                const Shell sh = B.shells[ck.x + si];
+                const Shell sh = load_shell(B.shells + ck.x + si);
                 if (sh.atom != last_atom) {
                     ++group;
                     last_atom = sh.atom;
-                    if ((group & 1) == half) {
+                    if (group % NG == half) {
                         const double X = x - B.atoms[4 * sh.atom];
                         const double Y = y - B.atoms[4 * sh.atom + 1];
                         const double Z = z - B.atoms[4 * sh.atom + 2];
@@ -437,7 +450,7 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                         Zf = dbl_to_flt_rn(Z);
                     }
                 }
-                if ((group & 1) != half) continue;
+                if (group % NG != half) continue;
                 const int nk = S.nkeep[ck.x + si];
                 if (nk == 0) continue;
                 float R0 = 0.f, R1 = 0.f;
@@ -505,15 +518,15 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
         if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
         phase ^= 1;
         tc_fence_after();
-        // epilogue: warp w reads TMEM lanes 32*(w%4).. (its 32 points), MO half w/4
+        // epilogue: warp w reads TMEM lanes 32*(w%4).. (its 32 points); the NG warps of
+        // a lane quarter take the 8-MO groups round-robin
         {
             const int q = warp & 3, h = warp >> 2;
-            const int nh = npad / 2;
             const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
             const float2* occf = D.occf + pass * npad;
             const float2* occ2f = D.occf + (D.npass + pass) * npad;
             double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
-            for (int m0 = h * nh; m0 < (h + 1) * nh; m0 += 8) {
+            for (int m0 = 8 * h; m0 < npad; m0 += 8 * NG) {
                 float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
                 tmem_ld8(tl + 0 * npad + m0, v0);
                 tmem_ld8(tl + 1 * npad + m0, h1);
@@ -545,20 +558,29 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
                 gc += flt_to_dbl(sc.hi) + flt_to_dbl(sc.lo);
             }
             const int pt = 32 * q + lane;
-            if (h == 1) {
-                red[pt] = racc;
-                red[M + pt] = ga;
-                red[2 * M + pt] = gb;
-                red[3 * M + pt] = gc;
+            // partial sums of groups 1..NG-1 go through the B operand buffer, free once
+            // the pass's MMAs are complete
+            double* red = (double*)S.B_s;
+            if (h > 0) {
+                red[((h - 1) * 4 + 0) * M + pt] = racc;
+                red[((h - 1) * 4 + 1) * M + pt] = ga;
+                red[((h - 1) * 4 + 2) * M + pt] = gb;
+                red[((h - 1) * 4 + 3) * M + pt] = gc;
             }
             tc_fence_before();
             __syncthreads();
             if (h == 0) {
                 // warp w < 4, lane l: point row 32 w + l == tid of this tile
-                rho_acc += racc + red[pt];
-                gx_acc += ga + red[M + pt];
-                gy_acc += gb + red[2 * M + pt];
-                gz_acc += gc + red[3 * M + pt];
+                for (int u = 1; u < NG; ++u) {
+                    racc += red[((u - 1) * 4 + 0) * M + pt];
+                    ga += red[((u - 1) * 4 + 1) * M + pt];
+                    gb += red[((u - 1) * 4 + 2) * M + pt];
+                    gc += red[((u - 1) * 4 + 3) * M + pt];
+                }
+                rho_acc += racc;
+                gx_acc += ga;
+                gy_acc += gb;
+                gz_acc += gc;
             }
             __syncthreads();
             tc_fence_after();
@@ -577,14 +599,15 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
 // CTA set-up shared by the kernels: shared-memory carve-up, A zeroed (columns of
 // screened shells keep stale but finite values, multiplied by zeroed B columns),
 // mbarrier, TMEM allocation.
+template <int NTT>
 __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_cols)
 {
     const int tid = threadIdx.x, warp = tid >> 5;
     CtaState S;
     S.A_s = smem;
     S.B_s = smem + A_BYTES;
-    S.red = (double*)(S.B_s + 3 * NMAX * 128);
-    S.kmask = (unsigned long long*)(S.red + 4 * M);
+    S.red = nullptr;
+    S.kmask = (unsigned long long*)(S.B_s + 3 * NMAX * 128);
     uint64_t* bar = (uint64_t*)(S.kmask + MAX_CHUNKS);
     uint32_t* tmem_slot = (uint32_t*)(bar + 1);
     S.abort_flag = (int*)(tmem_slot + 1);
@@ -592,7 +615,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
     S.bbox_part = S.bbox + 6;
     S.nkeep = (unsigned char*)(S.bbox_part + 24);
     S.bar_a = smem_u32(bar);
-    for (int i = tid; i < A_BYTES / 16; i += NT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < A_BYTES / 16; i += NTT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         mbar_init(S.bar_a, 1);
         *S.abort_flag = 0;
@@ -613,7 +636,8 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
 constexpr size_t SMEM_BYTES =
-    1024 + A_BYTES + 3 * NMAX * 128 + 4 * M * 8 + 8 * MAX_CHUNKS + 8 + 8 + 4 * 6 + 4 * 24 + MAX_SHELLS + 64;
+    1024 + A_BYTES + 3 * NMAX * 128 + 8 * MAX_CHUNKS + 8 + 8 + 4 * 6 + 4 * 24 + MAX_SHELLS + 64;
+static_assert(3 * 4 * 128 * 8 <= 3 * NMAX * 128, "epilogue partial sums must fit in the B operand buffer");
 static_assert(SMEM_BYTES <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 
 __device__ __forceinline__ void cta_teardown(const CtaState& S, uint32_t tm_cols)
@@ -648,11 +672,12 @@ inline void tiling(const Grid& g, MolDesc& D)
 
 extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
 
-__global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
+template <int NG>
+__global__ void __launch_bounds__(128 * NG, 1) rho_mixed_kernel(const Params P)
 {
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t tm_cols = tmem_cols_for(P.npad);
-    CtaState S = cta_setup(smem, tm_cols);
+    CtaState S = cta_setup<128 * NG>(smem, tm_cols);
     MolDesc D;
     D.B = P.B;
     D.g = P.g;
@@ -678,7 +703,7 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_kernel(const Params P)
         __syncthreads();
         const long long tile = next_tile;
         if (tile >= P.ntiles || *S.abort_flag) break;
-        mixed_tile(D, tile, S, phase, P.status);
+        mixed_tile<NG>(D, tile, S, phase, P.status);
     }
     cta_teardown(S, tm_cols);
 }
@@ -696,10 +721,11 @@ struct BatchParams {
     int* status;
 };
 
-__global__ void __launch_bounds__(NT, 1) rho_mixed_batch_kernel(const BatchParams P)
+template <int NG>
+__global__ void __launch_bounds__(128 * NG, 1) rho_mixed_batch_kernel(const BatchParams P)
 {
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    CtaState S = cta_setup(smem, 512);
+    CtaState S = cta_setup<128 * NG>(smem, 512);
     __shared__ MolDesc Dsh;
     __shared__ long long work;
     __shared__ int cur_mol;
@@ -726,7 +752,7 @@ __global__ void __launch_bounds__(NT, 1) rho_mixed_batch_kernel(const BatchParam
                 }
             }
             __syncthreads();
-            mixed_tile(Dsh, t - Dsh.tile0, S, phase, P.status);
+            mixed_tile<NG>(Dsh, t - Dsh.tile0, S, phase, P.status);
             if (*S.abort_flag) break;
         }
     }
@@ -784,6 +810,47 @@ __global__ void pack_occ_kernel(const double* __restrict__ occ, int nmo, int tot
 
 using namespace okg;
 
+namespace okg {
+namespace mx {
+// Shared-memory attribute of every instantiation (idempotent, called at set-up).
+static cudaError_t configure_kernels()
+{
+    cudaError_t e = cudaSuccess;
+    const int sm = (int)SMEM_BYTES;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rho_mixed_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rho_mixed_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rho_mixed_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return e;
+}
+
+static void launch_single(int ng, unsigned grid, cudaStream_t st, const Params& P)
+{
+    if (ng == 3)
+        rho_mixed_kernel<3><<<grid, 384, SMEM_BYTES, st>>>(P);
+    else if (ng == 4)
+        rho_mixed_kernel<4><<<grid, 512, SMEM_BYTES, st>>>(P);
+    else
+        rho_mixed_kernel<2><<<grid, 256, SMEM_BYTES, st>>>(P);
+}
+
+static void launch_batch(int ng, unsigned grid, cudaStream_t st, const BatchParams& P)
+{
+    if (ng == 3)
+        rho_mixed_batch_kernel<3><<<grid, 384, SMEM_BYTES, st>>>(P);
+    else if (ng == 4)
+        rho_mixed_batch_kernel<4><<<grid, 512, SMEM_BYTES, st>>>(P);
+    else
+        rho_mixed_batch_kernel<2><<<grid, 256, SMEM_BYTES, st>>>(P);
+}
+}  // namespace mx
+}  // namespace okg
+
 struct okg_mixed_plan {
     const okg_basis* basis;
     int nmo, npad, npass;
@@ -794,6 +861,7 @@ struct okg_mixed_plan {
     int* status;
     int sm_count;
     size_t smem;
+    int ngen;  // generation groups per point (threads per CTA = 128 x ngen)
 };
 
 extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_max, okg_mixed_plan** out);
@@ -838,13 +906,22 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     cudaMemset(p->status, 0, sizeof(int));
     p->sm_count = sms;
     p->smem = mx::SMEM_BYTES;
-    e = cudaFuncSetAttribute(mx::rho_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
+    p->ngen = mx::NG_DEFAULT;
+    e = mx::configure_kernels();
     if (e != cudaSuccess) {
         cudaFree(p->block);
         free(p);
         return cuda_status(e, "okg_mixed_plan_create: shared memory attribute");
     }
     *out = p;
+    return OKG_OK;
+}
+
+extern "C" int okg_mixed_plan_set_threads(okg_mixed_plan* p, int threads)
+{
+    if (!p || (threads != 256 && threads != 384 && threads != 512))
+        return set_error(OKG_ERR_ARG, "okg_mixed_plan_set_threads: threads must be 256, 384 or 512");
+    p->ngen = threads / 128;
     return OKG_OK;
 }
 
@@ -912,7 +989,7 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     P.nby = T.nby;
     P.nbz = T.nbz;
     const long long grid = P.ntiles < p->sm_count ? P.ntiles : p->sm_count;
-    mx::rho_mixed_kernel<<<(unsigned)grid, mx::NT, p->smem, (cudaStream_t)stream>>>(P);
+    mx::launch_single(p->ngen, (unsigned)grid, (cudaStream_t)stream, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
 }
 
@@ -927,6 +1004,7 @@ struct okg_batch {
     int grab;
     int ctas;
     size_t smem;
+    int ngen;
 };
 
 extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* grids, double* const* d_rho,
@@ -993,7 +1071,8 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
     b->grab = 1;
     b->ctas = b->sm_count;
     b->smem = mx::SMEM_BYTES;
-    e = cudaFuncSetAttribute(mx::rho_mixed_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    b->ngen = mx::NG_DEFAULT;
+    e = mx::configure_kernels();
     if (e != cudaSuccess) {
         cudaFree(b->block);
         free(b);
@@ -1011,12 +1090,15 @@ extern "C" int okg_batch_destroy(okg_batch* b)
     return cuda_status(e, "okg_batch_destroy");
 }
 
-extern "C" int okg_batch_set_schedule(okg_batch* b, int grab, int ctas)
+extern "C" int okg_batch_set_schedule(okg_batch* b, int grab, int ctas, int threads)
 {
     if (!b || grab < 1 || ctas < 1) return set_error(OKG_ERR_ARG, "okg_batch_set_schedule: grab and ctas >= 1");
     if (ctas > b->sm_count) return set_error(OKG_ERR_UNSUPPORTED, "okg_batch_set_schedule: one CTA per SM at most");
+    if (threads != 256 && threads != 384 && threads != 512)
+        return set_error(OKG_ERR_ARG, "okg_batch_set_schedule: threads must be 256, 384 or 512");
     b->grab = grab;
     b->ctas = ctas;
+    b->ngen = threads / 128;
     return OKG_OK;
 }
 
@@ -1042,7 +1124,7 @@ extern "C" int okg_batch_run(okg_batch* b, okg_stream stream)
     P.counter = b->d_counter;
     P.status = b->d_status;
     const long long grid = b->total_tiles < b->ctas ? b->total_tiles : b->ctas;
-    mx::rho_mixed_batch_kernel<<<(unsigned)grid, mx::NT, b->smem, st>>>(P);
+    mx::launch_batch(b->ngen, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_batch_run launch");
 }
 
@@ -1112,7 +1194,6 @@ struct NoallocDevice {
 static NoallocDevice g_noalloc_dev[64];
 static std::mutex g_noalloc_mu;
 
-static size_t noalloc_smem() { return SMEM_BYTES; }
 }  // namespace mx
 }  // namespace okg
 
@@ -1169,7 +1250,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
             void* ptr = nullptr;
             e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
             if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: cudaGetSymbolAddress");
-            e = cudaFuncSetAttribute(rho_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)noalloc_smem());
+            e = configure_kernels();
             if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: shared memory attribute");
             nd->base = (unsigned char*)ptr;
             nd->sm_count = sms;
@@ -1208,6 +1289,6 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     P.nby = T.nby;
     P.nbz = T.nbz;
     const long long grid = P.ntiles < nd->sm_count ? P.ntiles : nd->sm_count;
-    rho_mixed_kernel<<<(unsigned)grid, NT, noalloc_smem(), st>>>(P);
+    launch_single(NG_DEFAULT, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed_noalloc launch");
 }

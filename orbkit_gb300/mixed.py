@@ -29,6 +29,7 @@ _SIGS = {
     "okg_rho_mixed": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_lib.OkgGrid), ctypes.c_int, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "okg_mixed_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "okg_mixed_plan_set_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
 }
 
 
@@ -44,7 +45,7 @@ def _L():
 class MixedPlan:
     """Tensor-core operand form of a set of MO coefficients for one DeviceBasis."""
 
-    def __init__(self, basis, coeffs, occ, stream=None):
+    def __init__(self, basis, coeffs, occ, stream=None, threads=None):
         import torch
         self.basis = basis
         self._L = _L()
@@ -56,6 +57,15 @@ class MixedPlan:
         self._h = h
         self.C = C
         _lib.check(self._L.okg_mixed_set_coeffs(h, _lib.ptr(C), _lib.ptr(self.occ), _lib.stream_handle(stream)))
+        if threads is None:
+            import os
+            threads = int(os.environ.get("ORBKIT_GB300_MIXED_THREADS", "0")) or None
+        if threads:
+            self.set_threads(threads)
+
+    def set_threads(self, threads):
+        """Threads per CTA of the mixed kernel: 256, 384 or 512."""
+        _lib.check(self._L.okg_mixed_plan_set_threads(self._h, int(threads)))
 
     @property
     def handle(self):
