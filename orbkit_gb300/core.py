@@ -207,9 +207,29 @@ def cartesian2spherical(ao_list, ao_spec):
     return out.cpu().numpy().reshape((T.shape[0],) + shape[1:])
 
 
+def _mixed_rho(qc, x, y, z, vec, N, drv):
+    """rho (and grad rho) through the tensor-core mixed path."""
+    from .mixed import rho_grad
+    rho, grad = rho_grad(qc, x, y, z, vec)
+    rho = rho.reshape(N)
+    if drv is None:
+        return rho
+    return rho, grad.reshape((3,) + N)
+
+
+def _mixed_ok(calc_mo, drv, laplacian):
+    if calc_mo or laplacian:
+        return False
+    return drv is None or [validate_drv(d) for d in drv] == [1, 2, 3]
+
+
 def rho_compute(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, numproc=1, slice_length=1e4,
-                vector=None, save_hdf5=False, exact_mixed=False, **kwargs):
-    """Density, MOs, AOs or their derivatives on the grid module's grid (orbkit/core.py:314-605)."""
+                vector=None, save_hdf5=False, exact_mixed=False, precision="fp64", **kwargs):
+    """Density, MOs, AOs or their derivatives on the grid module's grid (orbkit/core.py:314-605).
+
+    precision="mixed" evaluates rho (drv=None) or rho and grad rho (drv=['x','y','z'])
+    on the tensor cores (orbkit_gb300.mixed, max relative rho error <= 1e-6); other
+    requests always run the FP64 path."""
     if calc_ao and calc_mo:
         raise ValueError("Choose either calc_ao=True or calc_mo=True")
     elif calc_ao:
@@ -227,6 +247,8 @@ def rho_compute(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, num
         grid.grid_init()
     vec = grid.is_vector
     x, y, z, vec, N = _grid_arrays(grid.x, grid.y, grid.z, vec, use_module=False)
+    if precision == "mixed" and _mixed_ok(calc_mo, drv, laplacian):
+        return _mixed_rho(qc, x, y, z, vec, N, drv)
     codes = [0] if drv is None else [validate_drv(d) for d in drv]
     if calc_mo:
         what = "ao" if calc_ao else "mo"
@@ -247,8 +269,8 @@ def rho_compute(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, num
 
 
 def rho_compute_no_slice(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, return_components=False,
-                         x=None, y=None, z=None, is_vector=None, exact_mixed=False, **kwargs):
-    """Unsliced variant with optional components (orbkit/core.py:607-839)."""
+                         x=None, y=None, z=None, is_vector=None, exact_mixed=False, precision="fp64", **kwargs):
+    """Unsliced variant with optional components (orbkit/core.py:607-839); precision as rho_compute."""
     if calc_ao and calc_mo:
         raise ValueError("calc_ao and calc_mo are mutually exclusive arguments."
                          "Use calc_mo and return_components instead!")
@@ -257,6 +279,8 @@ def rho_compute_no_slice(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=F
     if laplacian:
         drv = ["xx", "yy", "zz"]
     drv = _drv_list(drv)
+    if precision == "mixed" and not return_components and not calc_ao and _mixed_ok(calc_mo, drv, laplacian):
+        return _mixed_rho(qc, x, y, z, vec, N, drv)
     conv = lambda a: a if vec else a.reshape(a.shape[:-1] + N)
     if drv is not None:
         codes = [validate_drv(d) for d in drv]

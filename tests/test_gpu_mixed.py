@@ -93,3 +93,32 @@ def test_mixed_cusp_points_use_fp64(mixed):
     ro, go = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=8, nthreads=1)
     numpy.testing.assert_allclose(r, ro, rtol=1e-12)
     numpy.testing.assert_allclose(g, go, rtol=1e-11, atol=1e-12 * numpy.abs(go).max())
+
+
+def test_mixed_spherical_f_many_mos(mixed):
+    """Spherical basis with f shells and 100 MOs (two MO passes) on the mixed path."""
+    import okref
+    from orbkit_gb300 import synthetic
+    rng = numpy.random.default_rng(21)
+    el = ["C", "N", "O", "H", "C", "H", "C", "O", "H", "C"]
+    geo = synthetic.random_geometry(rng, len(el), 10.0)
+    ao = synthetic.build_basis(rng, el, with_f=True, spherical=True)
+    mo = synthetic.build_mos(rng, geo, ao, 100)
+    qc = synthetic.make_qc(geo, el, ao, mo)
+    p = rng.uniform(-6, 6, (3, 3000))
+    r, g = mixed.rho_grad(qc, p[0], p[1], p[2], True)
+    ro, go = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=128, nthreads=4)
+    _check(mixed, r, g, ro, go, "spherical f, 100 MOs")
+
+
+def test_mixed_through_drop_in_api(mixed):
+    """core.rho_compute(..., precision='mixed') routes rho / grad rho to the tensor-core path."""
+    from helpers import load_golden
+    from orbkit_gb300 import core, grid
+    qc, d = load_golden("h2o_molden.npz")
+    grid.set_grid(d["x"], d["y"], d["z"], is_vector=False)
+    r, dr = core.rho_compute(qc, drv=["x", "y", "z"], precision="mixed")
+    r64, dr64 = core.rho_compute(qc, drv=["x", "y", "z"])
+    _check(mixed, r.reshape(-1), dr.reshape(3, -1), r64.reshape(-1), dr64.reshape(3, -1), "drop-in")
+    assert core.rho_compute(qc, precision="mixed").shape == r64.shape
+    grid.reset_grid()
