@@ -76,15 +76,15 @@ struct BasisDev {
     const PrimMx* prim_mx;   // nprim (mixed path)
     const double* prim_adj;  // nprim x 2 : dw/dalpha, w/c (the alpha-dependent norm) for the adjoint
     const float* comp_g32;   // comp_g in FP32 (mixed path)
-    const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= 64 columns)
-    const int* mcol_cart;    // nmchunk x 64: listed Cartesian row feeding each column, or -1
+    const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= OKG_MKC columns)
+    const int* mcol_cart;    // nmchunk x OKG_MKC: listed Cartesian row feeding each column, or -1
     int natom, nshell, nprim, ncart, nsph, spherical;
     int max_nprim, nchunk, nmchunk;
 };
 
 // Mixed path: chunks of whole shells with at most OKG_MKC canonical columns
-// (one 128-byte swizzle atom of BF16 values).
-#define OKG_MKC 64
+// (one 64-byte swizzle row of BF16 values).
+#define OKG_MKC 32
 
 // Shells are grouped into chunks of at most KC listed Cartesian rows; the fused
 // kernels stage one chunk of AO values in shared memory at a time.

@@ -24,12 +24,22 @@
 //   * rho and grad rho accumulate the per-MO products in FP64.
 //
 // Tile: 128 grid points (the MMA's M), N = MO block padded to a multiple of 16
-// (<= 64 per pass), K = canonical Cartesian AO columns in chunks of 64 (one
-// 128-byte swizzle atom of BF16).  Per chunk the CTA writes 4 channels x 3 parts
-// of A (128 x 64 BF16, K-major, SWIZZLE_128B) into shared memory, copies the
-// matching pre-split, pre-swizzled B block, and one thread issues 96 MMAs.
-// Accumulators: 8 x N FP32 columns of TMEM (value: 4 leading + 1 correction;
-// d/dx, d/dy, d/dz).  Persistent CTAs, one per SM.
+// (<= 64 per pass), K = canonical Cartesian AO columns in chunks of 32 (one
+// 64-byte swizzle row of BF16).  Persistent CTAs, one per SM, each with
+// 128 x NG generation threads (NG threads per grid point) and one MMA warp,
+// connected by a two-stage ring in shared memory:
+//   * generation threads write 4 channels x 3 parts of A (128 x 32 BF16, K-major,
+//     SWIZZLE_64B) for a chunk into a free stage and arrive on its "full" barrier;
+//   * the MMA warp bulk-copies the chunk's pre-split, pre-swizzled B block into the
+//     stage (columns of screened shells then zeroed), waits for "full", issues 48 MMAs
+//     from one thread and commits them to the stage's "empty" barrier, so the
+//     tensor core works on one chunk while the next one is generated;
+//   * after the last chunk of an MO pass the MMA warp commits to "acc full"; the
+//     generation warps read the accumulators (8 x N FP32 columns of TMEM: value
+//     4 leading + 1 correction; d/dx, d/dy, d/dz), arrive on "acc empty" and
+//     reduce in FP64, each warp owning whole outputs (rho, or one gradient
+//     component) of its 32 points.
+// Every wait is bounded and raises the status word instead of hanging.
 #include <stdio.h>
 
 #include <cuda_bf16.h>
@@ -42,19 +52,23 @@ namespace okg {
 namespace mx {
 
 constexpr int M = 128;
-constexpr int KC = OKG_MKC;           // 64 BF16 = 128 bytes
-constexpr int NG_DEFAULT = 4;         // generation groups per point (threads = 128 x groups); 512 threads measured fastest on the mid workload
-constexpr int A_TILE = M * 128;       // bytes of one 128 x 64 BF16 sub-tile
-constexpr int A_BYTES = 12 * A_TILE;  // 4 channels x 3 parts
+constexpr int KC = OKG_MKC;           // 32 BF16 = 64 bytes
+constexpr int ROWB = KC * 2;          // bytes of one operand row
+constexpr int RUNITS = ROWB / 16;     // 16-byte units of one operand row
+constexpr int NG_DEFAULT = 4;         // generation groups per point (generation threads = 128 x groups)
+constexpr int A_TILE = M * ROWB;      // bytes of one 128 x 32 BF16 sub-tile
+constexpr int A_STAGE = 12 * A_TILE;  // 4 channels x 3 parts
 constexpr int NMAX = 64;              // MO columns per pass
+constexpr int B_STAGE = 3 * NMAX * ROWB;
+constexpr int NSTAGE = 2;
 constexpr long long WAIT_LIMIT = 1ll << 24;
 
 struct Params {
     BasisDev B;
     Grid g;
-    const uint4* bpack;    // [npass][nmchunk][3][npad x 128 B], pre-swizzled
+    const uint4* bpack;    // [npass][nmchunk][3][npad x 64 B], pre-swizzled
     const double* occ;     // [npass * npad], zero padded
-    int npass, npad;
+    int npass, npad, nmo;
     int want_grad;
     double* rho;
     double* grad;          // 3 x ld
@@ -70,15 +84,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p)
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// SMEM matrix descriptor: K-major, SWIZZLE_128B, SBO = 1024 B (8-row group stride).
+// SMEM matrix descriptor: K-major, SWIZZLE_64B, SBO = 512 B (8-row group stride).
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr)
 {
     uint64_t d = 0;
     d |= (uint64_t)((addr >> 4) & 0x3FFF);
     d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+    d |= (uint64_t)(8 * ROWB >> 4) << 32;   // stride byte offset
     d |= (uint64_t)1 << 46;                 // descriptor version
-    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    d |= (uint64_t)4 << 61;                 // SWIZZLE_64B
     return d;
 }
 
@@ -126,6 +140,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* st
         if (mbar_try(bar, parity)) return true;
     atomicExch(status, 1);
     return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// One bulk copy global -> shared (16-byte aligned addresses, size a multiple of
+// 16) completing on an mbarrier that expects `bytes` transaction bytes.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
 }
 
 __device__ __forceinline__ void fence_proxy_async()
@@ -200,17 +229,19 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& b0, __nv_bfloat16
     b2 = __float2bfloat16_rn(r2);
 }
 
-// byte offset of element (row m, column k) in a 128 x 64 BF16 K-major SW128 tile
-__device__ __forceinline__ uint32_t sw128_off(int m, int k)
+// byte offset of element (row m, column k) in a K-major BF16 tile with 32-element
+// rows and SWIZZLE_64B: 8-row groups of 512 B, the 16-byte unit index XORed with
+// address bits 7..8, i.e. (m >> 1) & 3
+__host__ __device__ __forceinline__ uint32_t sw64_off(int m, int k)
 {
-    return (uint32_t)((m >> 3) * 1024 + (m & 7) * 128 + ((((k >> 3) ^ (m & 7)) & 7) << 4) + ((k & 7) << 1));
+    return (uint32_t)((m >> 3) * 512 + (m & 7) * 64 + ((((k >> 3) ^ (m >> 1)) & 3) << 4) + ((k & 7) << 1));
 }
 
 // One molecule as seen by a tile: its basis tables, grid, coefficient tiles and outputs.
 struct MolDesc {
     BasisDev B;
     Grid g;
-    const uint4* bpack;  // [npass][nmchunk][3][npad x 128 B], pre-swizzled
+    const uint4* bpack;  // [npass][nmchunk][3][npad x 64 B], pre-swizzled
     const double* occ;   // [npass * npad] occupations, then [npass * npad] 2 x occupations (zero padded)
     const float2* occf;  // the same 2 x npass x npad values as double-float (hi, lo) pairs
     double* rho;
@@ -219,6 +250,7 @@ struct MolDesc {
     long long tile0;     // first tile of this molecule in the batch's tile numbering
     long long ntiles;
     int npass, npad;
+    int nmo;             // MO columns beyond nmo (last pass) are zero padding
     int want_grad;
     int brick;           // regular grid covered by 4 x 4 x 8 bricks (else runs of 128 flattened points)
     int nby, nbz;        // bricks along y and z
@@ -231,22 +263,32 @@ constexpr float SCREEN_LOG2 = 64.0f;
 
 // Shared-memory pieces of the CTA used by every tile.
 struct CtaState {
-    unsigned char* A_s;
-    unsigned char* B_s;
-    double* red;
-    uint32_t bar_a;
+    unsigned char* A_s;          // NSTAGE x A_STAGE
+    unsigned char* B_s;          // NSTAGE x B_STAGE
+    uint32_t bar_full;           // NSTAGE mbarriers, 8 B apart: stage written by every generation thread
+    uint32_t bar_empty;          // NSTAGE mbarriers: the stage's MMAs are complete (tcgen05.commit)
+    uint32_t bar_bload;          // NSTAGE mbarriers: the stage's B block has landed (bulk copy)
+    uint32_t bar_acc_full;       // accumulators of an MO pass complete (tcgen05.commit)
+    uint32_t bar_acc_empty;      // every generation thread has read the accumulators
     uint32_t tmem;
     int* abort_flag;
     float* bbox;                 // lo x,y,z, hi x,y,z of the current tile
     float* bbox_part;            // 4 warps x 6
     unsigned char* nkeep;        // per shell: primitives kept for the current tile
-    unsigned long long* kmask;   // per chunk: columns whose shell is kept for the current tile
+    unsigned* kmask;             // per chunk: columns whose shell is kept for the current tile
+};
+
+// Position in the CTA's stream of chunks and MO passes; the generation threads and
+// the MMA warp each keep a copy and advance it identically.
+struct Pipe {
+    uint32_t seq = 0;  // chunks issued so far (stage = seq % 2, use = seq / 2)
+    uint32_t acc = 0;  // MO passes whose accumulators were handed over so far
 };
 
 // Per-tile screening tables live in shared memory: at most MAX_SHELLS shells and
 // MAX_CHUNKS chunks per molecule on the mixed path.
 constexpr int MAX_SHELLS = 2048;
-constexpr int MAX_CHUNKS = 128;
+constexpr int MAX_CHUNKS = 256;
 
 // FP64 <-> FP32 without the FP64 pipe: rounding double -> float and exact
 // float -> double through integer operations on the IEEE bit patterns.
@@ -328,33 +370,272 @@ __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int
     return true;
 }
 
-// The whole computation of one 128-point tile of one molecule: bounding box, then
-// per MO pass and chunk: screening, B copy (screened columns zeroed), A generation
-// for kept shells, 96 MMAs; the FP64 epilogue; the stores.
+// Generation side of one tile (threads 0 .. 128 NG - 1): per MO pass and kept
+// chunk, the AO values of this thread's atoms at its point into a free stage; per
+// pass the epilogue over this warp's outputs; at the end the stores.
 template <int NG>
-__device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, const CtaState& S, uint32_t& phase,
-                                           int* status)
+__device__ __forceinline__ void gen_tile(const MolDesc& D, const CtaState& S, Pipe& pp, int* status, bool valid,
+                                         long long p, double x, double y, double z)
 {
-    constexpr int NTT = 128 * NG;
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
     const int lane = tid & 31;
     const int prow = tid & (M - 1);  // point row of this thread in the tile
-    const int half = tid >> 7;       // generation group: atoms of a chunk go round-robin to the NG groups
+    const int grp = tid >> 7;        // generation group: atom runs of a pass go round-robin to the NG groups
+    const BasisDev& B = D.B;
+    const int npad = D.npad;
+    const unsigned chmask = D.want_grad ? 0xFu : 0x1u;
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its 32 points = rows prow) and
+    // owns the outputs o (0 = rho, 1..3 = d/dx, d/dy, d/dz) with o % NG == w / 4
+    const int q = warp & 3, h = warp >> 2;
+    bool own[4];
+#pragma unroll
+    for (int o = 0; o < 4; ++o) own[o] = (o % NG == h) && (o == 0 || D.want_grad);
+    const bool any_own = own[0] || own[1] || own[2] || own[3];
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+
+    for (int pass = 0; pass < D.npass; ++pass) {
+        int nchunks = 0;
+        int last_atom = -1, ord = -1;
+        bool mine = false;
+        double rr = 0;
+        float Xf = 0, Yf = 0, Zf = 0;
+        for (int c = 0; c < B.nmchunk; ++c) {
+            if (S.kmask[c] == 0u) continue;  // nothing of this chunk reaches the tile
+            const uint32_t s = pp.seq & 1u, u = pp.seq >> 1;
+            unsigned char* A_s = S.A_s + s * A_STAGE;
+            if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
+            const int4 ck = B.mchunks[c];
+            for (int si = ck.x; si < ck.y; ++si) {
+                const Shell sh = load_shell(B.shells + si);
+                if (sh.atom != last_atom) {
+                    last_atom = sh.atom;
+                    ++ord;
+                    mine = ord % NG == grp;
+                    if (mine) {
+                        const double X = x - B.atoms[4 * sh.atom];
+                        const double Y = y - B.atoms[4 * sh.atom + 1];
+                        const double Z = z - B.atoms[4 * sh.atom + 2];
+                        rr = X * X + Y * Y + Z * Z;
+                        Xf = dbl_to_flt_rn(X);
+                        Yf = dbl_to_flt_rn(Y);
+                        Zf = dbl_to_flt_rn(Z);
+                    }
+                }
+                if (!mine) continue;
+                const int nk = S.nkeep[si];
+                if (nk == 0) continue;
+                float R0 = 0.f, R1 = 0.f;
+                for (int k = 0; k < nk; ++k) {
+                    const PrimMx pm = B.prim_mx[sh.prim0 + k];
+                    const float e = exp2_neg(pm.a2 * rr);
+                    R0 = fmaf(pm.w, e, R0);
+                    R1 = fmaf(pm.wa, e, R1);
+                }
+                const Radial<float> r{R0, R1, 0.f};
+                shell_eval_L(sh.L, Xf, Yf, Zf, r, chmask, false, [&](int ch, int j, float v) {
+                    v *= B.comp_g32[sh.comp0 + j];
+                    __nv_bfloat16 b0, b1, b2;
+                    split3(v, b0, b1, b2);
+                    unsigned char* base = A_s + ch * 3 * A_TILE + sw64_off(prow, sh.mcol + j);
+                    *(__nv_bfloat16*)(base) = b0;
+                    *(__nv_bfloat16*)(base + A_TILE) = b1;
+                    *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
+                });
+            }
+            fence_proxy_async();
+            mbar_arrive(S.bar_full + 8 * s);
+            ++pp.seq;
+            ++nchunks;
+        }
+        if (nchunks == 0) continue;  // no AO of any chunk reaches this tile: this pass contributes zero
+        const uint32_t P = pp.acc++;
+        if (!mbar_wait(S.bar_acc_full, P & 1u, status)) *S.abort_flag = 1;
+        tc_fence_after();
+        if (any_own) {
+            const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
+            const float2* occf = D.occf + pass * npad;
+            const float2* occ2f = D.occf + (D.npass + pass) * npad;
+            const int nlead = 2 * nchunks < 4 ? 2 * nchunks : 4;  // leading accumulators written in this pass
+            int mo_end = D.nmo - pass * npad;
+            mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
+            for (int m0 = 0; m0 < mo_end; m0 += 8) {
+                float v[8], a1[8], a2[8], a3[8], lo[8];
+                tmem_ld8(tl + 0 * npad + m0, v);
+                tmem_ld8(tl + 1 * npad + m0, a1);
+                tmem_ld8(tl + 2 * npad + m0, a2);
+                tmem_ld8(tl + 3 * npad + m0, a3);
+                tmem_ld8(tl + 4 * npad + m0, lo);
+                tmem_wait_ld();
+                if (nlead < 4) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        a2[i] = nlead > 2 ? a2[i] : 0.f;
+                        a3[i] = 0.f;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = ((v[i] + a1[i]) + (a2[i] + a3[i])) + lo[i];
+                // sum_i occ_i v_i^2 and sum_i 2 occ_i v_i vd_i over the 8 MOs in double-float
+                // FP32 arithmetic (exact products by FMA, two-sum accumulation, about 44
+                // bits), then the group sums are added to the FP64 accumulators
+                if (own[0]) {
+                    DF sr;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) sr.add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
+                    acc[0] += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
+                }
+#pragma unroll
+                for (int o = 1; o < 4; ++o) {
+                    if (!own[o]) continue;
+                    float vd[8];
+                    tmem_ld8(tl + (4 + o) * npad + m0, vd);
+                    tmem_wait_ld();
+                    DF sd;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
+                    acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
+                }
+            }
+        }
+        tc_fence_before();
+        mbar_arrive(S.bar_acc_empty);
+    }
+    (void)lane;
+    if (valid && !*S.abort_flag) {
+        if (own[0]) D.rho[p] = acc[0];
+#pragma unroll
+        for (int o = 1; o < 4; ++o)
+            if (own[o]) D.grad[(long long)(o - 1) * D.ld + p] = acc[o];
+    }
+}
+
+// MMA side of one tile (the last warp): per MO pass and kept chunk, the masked B
+// copy into the stage, then 48 MMAs (or 12 without gradient) from lane 0 once the
+// generation threads filled the stage.
+__device__ __forceinline__ void mma_tile(const MolDesc& D, const CtaState& S, Pipe& pp, int* status)
+{
+    const int lane = threadIdx.x & 31;
     const BasisDev& B = D.B;
     const int npad = D.npad;
     const uint32_t idesc = idesc_bf16(M, npad);
-    const int bunits = 3 * npad * 8;  // 16-byte units of one B block
-    unsigned char* A_s = S.A_s;
-    unsigned char* B_s = S.B_s;
+    const int bunits = 3 * npad * RUNITS;  // 16-byte units of one B block
+    const int nch = D.want_grad ? 4 : 1;
+    const uint32_t bpart16 = (uint32_t)(npad * ROWB) >> 4;
+    for (int pass = 0; pass < D.npass; ++pass) {
+        int kq = 0;  // K-steps issued in this pass
+        for (int c = 0; c < B.nmchunk; ++c) {
+            const unsigned km = S.kmask[c];
+            if (km == 0u) continue;
+            const uint32_t s = pp.seq & 1u, u = pp.seq >> 1;
+            unsigned char* B_s = S.B_s + s * B_STAGE;
+            // B block of this (pass, chunk) by one bulk copy once the stage is free
+            if (lane == 0) {
+                if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
+                bulk_load(smem_u32(B_s), D.bpack + ((long long)pass * B.nmchunk + c) * bunits, (uint32_t)bunits * 16u,
+                          S.bar_bload + 8 * s);
+            }
+            __syncwarp();
+            if (!mbar_wait(S.bar_bload + 8 * s, u & 1u, status)) *S.abort_flag = 1;
+            // columns of screened shells are zeroed.  Lane l touches the 16-byte units
+            // l, l + 32, ...: rows n = l / 4 (mod 8) of every part, physical unit l % 4, so
+            // with rows of 4 units and the 64-byte swizzle (unit ^ (n >> 1) % 4) always the
+            // same logical 8-column group
+            const unsigned m8 = (km >> (8 * ((lane & 3) ^ ((lane >> 3) & 3)))) & 0xFFu;
+            if (m8 != 0xFFu) {
+                unsigned keep[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    keep[t] = ((m8 >> (2 * t)) & 1u ? 0x0000FFFFu : 0u) | ((m8 >> (2 * t + 1)) & 1u ? 0xFFFF0000u : 0u);
+                for (int i = lane; i < bunits; i += 32) {
+                    const uint4 v = ((const uint4*)B_s)[i];
+                    ((uint4*)B_s)[i] = make_uint4(v.x & keep[0], v.y & keep[1], v.z & keep[2], v.w & keep[3]);
+                }
+                fence_proxy_async();
+            }
+            __syncwarp();
+            if (lane == 0) {
+                // the previous pass's accumulators must have been read before they are overwritten
+                if (kq == 0 && pp.acc > 0 && !mbar_wait(S.bar_acc_empty, (pp.acc - 1) & 1u, status))
+                    *S.abort_flag = 1;
+                if (!mbar_wait(S.bar_full + 8 * s, u & 1u, status)) *S.abort_flag = 1;
+                tc_fence_after();
+                if (!*S.abort_flag) {
+                    // descriptors differ only in the start-address field (bytes >> 4)
+                    const uint64_t adesc = sdesc(smem_u32(S.A_s + s * A_STAGE)), bdesc = sdesc(smem_u32(B_s));
+#pragma unroll 1
+                    for (int ch = 0; ch < nch; ++ch) {
+#pragma unroll
+                        for (int k = 0; k < KC / 16; ++k) {
+                            const int ks = kq + k;
+                            // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
+                            const int pa[6] = {0, 0, 1, 0, 1, 2};
+                            const int pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+                            for (int t = 0; t < 6; ++t) {
+                                const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 32) >> 4);
+                                const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
+                                uint32_t col, accf;
+                                if (ch == 0 && t == 0) {  // leading product -> accumulator ks mod 4
+                                    col = ks & 3;
+                                    accf = ks >= 4;
+                                } else if (ch == 0) {     // value corrections -> accumulator 4
+                                    col = 4;
+                                    accf = ks > 0 || t > 1;
+                                } else {                  // gradient channel ch -> accumulator 4 + ch
+                                    col = 4 + ch;
+                                    accf = ks > 0 || t > 0;
+                                }
+                                mma_bf16(S.tmem + col * npad, ad, bd, idesc, accf);
+                            }
+                        }
+                    }
+                    mma_commit(S.bar_empty + 8 * s);
+                } else {
+                    mbar_arrive(S.bar_empty + 8 * s);
+                }
+            }
+            __syncwarp();
+            ++pp.seq;
+            kq += KC / 16;
+        }
+        if (kq > 0) {
+            if (lane == 0) {
+                if (!*S.abort_flag)
+                    mma_commit(S.bar_acc_full);
+                else
+                    mbar_arrive(S.bar_acc_full);
+            }
+            __syncwarp();
+            ++pp.acc;
+        }
+    }
+}
 
-    long long p;
-    const bool valid = tile_point(D, tile, prow, p);
-    double x, y, z;
-    grid_point(D.g, p, x, y, z);
+// One 128-point tile of one molecule (every thread of the CTA): bounding box and
+// screening of every shell against it, then the generation threads and the MMA
+// warp each run their side.
+template <int NG>
+__device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, const CtaState& S, Pipe& pp,
+                                           int* status)
+{
+    constexpr int NTG = 128 * NG;  // generation threads
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
+    const bool gen = tid < NTG;
+    const int prow = tid & (M - 1);
+    const BasisDev& B = D.B;
 
+    long long p = 0;
+    bool valid = false;
+    double x = 0, y = 0, z = 0;
+    if (gen) {
+        valid = tile_point(D, tile, prow, p);
+        grid_point(D.g, p, x, y, z);
+    }
     // bounding box of the tile's valid points (rows 0..127 = warps 0..3)
-    {
+    if (warp < 4) {
         float v[6];
         v[0] = valid ? dbl_to_flt_rn(x) : 3.0e38f;
         v[1] = valid ? dbl_to_flt_rn(y) : 3.0e38f;
@@ -369,255 +650,73 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
 #pragma unroll
             for (int c = 3; c < 6; ++c) v[c] = fmaxf(v[c], __shfl_xor_sync(0xffffffffu, v[c], o));
         }
-        if (warp < 4 && lane == 0)
+        if (lane == 0)
             for (int c = 0; c < 6; ++c) S.bbox_part[warp * 6 + c] = v[c];
-        __syncthreads();
-        if (tid < 6) {
-            float a = S.bbox_part[tid];
-            for (int w = 1; w < 4; ++w)
-                a = tid < 3 ? fminf(a, S.bbox_part[w * 6 + tid]) : fmaxf(a, S.bbox_part[w * 6 + tid]);
-            S.bbox[tid] = a;
-        }
     }
+    __syncthreads();
+    if (tid < 6) {
+        float a = S.bbox_part[tid];
+        for (int w = 1; w < 4; ++w)
+            a = tid < 3 ? fminf(a, S.bbox_part[w * 6 + tid]) : fmaxf(a, S.bbox_part[w * 6 + tid]);
+        S.bbox[tid] = a;
+    }
+    if (gen)
+        for (int c = tid; c < B.nmchunk; c += NTG) S.kmask[c] = 0u;
+    __syncthreads();
     // screening of every shell against the tile's bounding box, once per tile
-    for (int c = tid; c < B.nmchunk; c += NTT) S.kmask[c] = 0ull;
+    if (gen) {
+        for (int si = tid; si < B.nshell; si += NTG) {
+            const Shell sh = load_shell(B.shells + si);
+            const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
+                        az = (float)B.atoms[4 * sh.atom + 2];
+            const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
+            const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
+            const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            int nk = 0;
+            while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+            S.nkeep[si] = (unsigned char)nk;
+            if (nk > 0) atomicOr(S.kmask + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
+        }
+    }
     __syncthreads();
-    for (int si = tid; si < B.nshell; si += NTT) {
-        const Shell sh = load_shell(B.shells + si);
-        const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
-                    az = (float)B.atoms[4 * sh.atom + 2];
-        const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
-        const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
-        const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        int nk = 0;
-        while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
-        S.nkeep[si] = (unsigned char)nk;
-        if (nk > 0) atomicOr(S.kmask + sh.mchunk, ((1ull << ncanon(sh.L)) - 1ull) << sh.mcol);
-    }
-    __syncthreads();
-    double rho_acc = 0.0, gx_acc = 0.0, gy_acc = 0.0, gz_acc = 0.0;
-
-    for (int pass = 0; pass < D.npass; ++pass) {
-        bool pending = false;  // MMAs committed and not yet waited for
-        bool issued = false;   // some chunk of this pass reached the tensor core
-        for (int c = 0; c < B.nmchunk; ++c) {
-            const int4 ck = B.mchunks[c];
-            const int ns = ck.y - ck.x;
-            const unsigned long long km = S.kmask[c];
-            if (km == 0ull) continue;  // nothing of this chunk reaches the tile
-            if (pending) {             // previous chunk's MMAs must be done before A/B are overwritten
-                if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
-                phase ^= 1;
-                pending = false;
-            }
-            // B block of this (pass, chunk); columns of screened shells are zeroed
-            const uint4* src = D.bpack + ((long long)pass * B.nmchunk + c) * bunits;
-            for (int i = tid; i < bunits; i += NTT) {
-                uint4 v = src[i];
-                const int n = (i >> 3) % npad;
-                const int lc = (i & 7) ^ (n & 7);  // logical 8-column group of this 16-byte unit
-                const unsigned m8 = (unsigned)(km >> (8 * lc)) & 0xFFu;
-                if (m8 != 0xFFu) {
-                    unsigned w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const unsigned keep = ((m8 >> (2 * q)) & 1u ? 0x0000FFFFu : 0u) |
-                                              ((m8 >> (2 * q + 1)) & 1u ? 0xFFFF0000u : 0u);
-                        w[q] &= keep;
-                    }
-                    v = make_uint4(w[0], w[1], w[2], w[3]);
-                }
-                ((uint4*)B_s)[i] = v;
-            }
-            // A: AO values of this chunk's kept shells for this thread's point; atoms
-            // (runs of shells on one atom) alternate between the two halves
-            int last_atom = -1, group = -1;
-            double rr = 0;
-            float Xf = 0, Yf = 0, Zf = 0;
-            for (int si = 0; si < ns; ++si) {
-                const Shell sh = load_shell(B.shells + ck.x + si);
-                if (sh.atom != last_atom) {
-                    ++group;
-                    last_atom = sh.atom;
-                    if (group % NG == half) {
-                        const double X = x - B.atoms[4 * sh.atom];
-                        const double Y = y - B.atoms[4 * sh.atom + 1];
-                        const double Z = z - B.atoms[4 * sh.atom + 2];
-                        rr = X * X + Y * Y + Z * Z;
-                        Xf = dbl_to_flt_rn(X);
-                        Yf = dbl_to_flt_rn(Y);
-                        Zf = dbl_to_flt_rn(Z);
-                    }
-                }
-                if (group % NG != half) continue;
-                const int nk = S.nkeep[ck.x + si];
-                if (nk == 0) continue;
-                float R0 = 0.f, R1 = 0.f;
-                for (int q = 0; q < nk; ++q) {
-                    const PrimMx pm = B.prim_mx[sh.prim0 + q];
-                    const float e = exp2_neg(pm.a2 * rr);
-                    R0 = fmaf(pm.w, e, R0);
-                    R1 = fmaf(pm.wa, e, R1);
-                }
-                const Radial<float> r{R0, R1, 0.f};
-                shell_eval_L(sh.L, Xf, Yf, Zf, r, 0xFu, false, [&](int ch, int j, float v) {
-                    v *= B.comp_g32[sh.comp0 + j];
-                    __nv_bfloat16 b0, b1, b2;
-                    split3(v, b0, b1, b2);
-                    const uint32_t off = sw128_off(prow, sh.mcol + j);
-                    unsigned char* base = A_s + ch * 3 * A_TILE + off;
-                    *(__nv_bfloat16*)(base) = b0;
-                    *(__nv_bfloat16*)(base + A_TILE) = b1;
-                    *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
-                });
-            }
-            fence_proxy_async();
-            __syncthreads();
-            if (tid == 0 && !*S.abort_flag) {
-                tc_fence_after();
-                // descriptors differ only in the start-address field (bytes >> 4)
-                const uint64_t adesc = sdesc(smem_u32(A_s)), bdesc = sdesc(smem_u32(B_s));
-                const uint32_t bpart16 = (uint32_t)(npad * 128) >> 4;
-                const uint32_t first = issued ? 0u : 1u;
-#pragma unroll 1
-                for (int ch = 0; ch < 4; ++ch) {
-#pragma unroll
-                    for (int k = 0; k < KC / 16; ++k) {
-                        // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
-                        const int pa[6] = {0, 0, 1, 0, 1, 2};
-                        const int pb[6] = {0, 1, 0, 2, 1, 0};
-#pragma unroll
-                        for (int t = 0; t < 6; ++t) {
-                            const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 32) >> 4);
-                            const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
-                            uint32_t col, acc;
-                            if (ch == 0 && t == 0) {         // leading product -> accumulator k
-                                col = k;
-                                acc = !first;
-                            } else if (ch == 0) {            // value corrections -> accumulator 4
-                                col = 4;
-                                acc = !first || k > 0 || t > 1;
-                            } else {                         // gradient channel ch -> accumulator 4 + ch
-                                col = 4 + ch;
-                                acc = !first || k > 0 || t > 0;
-                            }
-                            mma_bf16(S.tmem + col * npad, ad, bd, idesc, acc);
-                        }
-                    }
-                }
-                mma_commit(S.bar_a);
-            } else if (tid == 0) {
-                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(S.bar_a) : "memory");
-            }
-            pending = true;
-            issued = true;
-        }
-        if (!issued) continue;  // no AO of any chunk reaches this tile: this pass contributes zero
-        // accumulators of this pass complete
-        if (!mbar_wait(S.bar_a, phase, status)) *S.abort_flag = 1;
-        phase ^= 1;
-        tc_fence_after();
-        // epilogue: warp w reads TMEM lanes 32*(w%4).. (its 32 points); the NG warps of
-        // a lane quarter take the 8-MO groups round-robin
-        {
-            const int q = warp & 3, h = warp >> 2;
-            const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
-            const float2* occf = D.occf + pass * npad;
-            const float2* occ2f = D.occf + (D.npass + pass) * npad;
-            double racc = 0.0, ga = 0.0, gb = 0.0, gc = 0.0;
-            for (int m0 = 8 * h; m0 < npad; m0 += 8 * NG) {
-                float v0[8], v1[8], v2[8], v3[8], h1[8], h2[8], h3[8], lo[8];
-                tmem_ld8(tl + 0 * npad + m0, v0);
-                tmem_ld8(tl + 1 * npad + m0, h1);
-                tmem_ld8(tl + 2 * npad + m0, h2);
-                tmem_ld8(tl + 3 * npad + m0, h3);
-                tmem_ld8(tl + 4 * npad + m0, lo);
-                tmem_ld8(tl + 5 * npad + m0, v1);
-                tmem_ld8(tl + 6 * npad + m0, v2);
-                tmem_ld8(tl + 7 * npad + m0, v3);
-                tmem_wait_ld();
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v0[i] = ((v0[i] + h1[i]) + (h2[i] + h3[i])) + lo[i];
-                // sum_i occ_i v0_i^2 and sum_i 2 occ_i v0_i vd_i over the 8 MOs in double-float
-                // FP32 arithmetic (exact products by FMA, two-sum accumulation, about 44
-                // bits), then add the group sums to the FP64 accumulators
-                DF sr, sa, sb, sc;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const float2 o = __ldg(occf + m0 + i);
-                    const float2 o2 = __ldg(occ2f + m0 + i);
-                    sr.add(df_mul(o, v0[i], v0[i]));
-                    sa.add(df_mul(o2, v0[i], v1[i]));
-                    sb.add(df_mul(o2, v0[i], v2[i]));
-                    sc.add(df_mul(o2, v0[i], v3[i]));
-                }
-                racc += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
-                ga += flt_to_dbl(sa.hi) + flt_to_dbl(sa.lo);
-                gb += flt_to_dbl(sb.hi) + flt_to_dbl(sb.lo);
-                gc += flt_to_dbl(sc.hi) + flt_to_dbl(sc.lo);
-            }
-            const int pt = 32 * q + lane;
-            // partial sums of groups 1..NG-1 go through the B operand buffer, free once
-            // the pass's MMAs are complete
-            double* red = (double*)S.B_s;
-            if (h > 0) {
-                red[((h - 1) * 4 + 0) * M + pt] = racc;
-                red[((h - 1) * 4 + 1) * M + pt] = ga;
-                red[((h - 1) * 4 + 2) * M + pt] = gb;
-                red[((h - 1) * 4 + 3) * M + pt] = gc;
-            }
-            tc_fence_before();
-            __syncthreads();
-            if (h == 0) {
-                // warp w < 4, lane l: point row 32 w + l == tid of this tile
-                for (int u = 1; u < NG; ++u) {
-                    racc += red[((u - 1) * 4 + 0) * M + pt];
-                    ga += red[((u - 1) * 4 + 1) * M + pt];
-                    gb += red[((u - 1) * 4 + 2) * M + pt];
-                    gc += red[((u - 1) * 4 + 3) * M + pt];
-                }
-                rho_acc += racc;
-                gx_acc += ga;
-                gy_acc += gb;
-                gz_acc += gc;
-            }
-            __syncthreads();
-            tc_fence_after();
-        }
-    }
-    if (tid < M && valid && !*S.abort_flag) {
-        D.rho[p] = rho_acc;
-        if (D.want_grad) {
-            D.grad[p] = gx_acc;
-            D.grad[D.ld + p] = gy_acc;
-            D.grad[2 * D.ld + p] = gz_acc;
-        }
-    }
+    if (gen)
+        gen_tile<NG>(D, S, pp, status, valid, p, x, y, z);
+    else
+        mma_tile(D, S, pp, status);
 }
 
-// CTA set-up shared by the kernels: shared-memory carve-up, A zeroed (columns of
-// screened shells keep stale but finite values, multiplied by zeroed B columns),
-// mbarrier, TMEM allocation.
-template <int NTT>
+// CTA set-up shared by the kernels: shared-memory carve-up, A stages zeroed
+// (columns of screened shells keep stale but finite values, multiplied by zeroed B
+// columns), mbarriers, TMEM allocation.  NTT threads in all, NTG of them generate.
+template <int NTT, int NTG>
 __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_cols)
 {
     const int tid = threadIdx.x, warp = tid >> 5;
     CtaState S;
     S.A_s = smem;
-    S.B_s = smem + A_BYTES;
-    S.red = nullptr;
-    S.kmask = (unsigned long long*)(S.B_s + 3 * NMAX * 128);
-    uint64_t* bar = (uint64_t*)(S.kmask + MAX_CHUNKS);
-    uint32_t* tmem_slot = (uint32_t*)(bar + 1);
+    S.B_s = smem + NSTAGE * A_STAGE;
+    S.kmask = (unsigned*)(S.B_s + NSTAGE * B_STAGE);
+    uint64_t* bar = (uint64_t*)(S.kmask + MAX_CHUNKS);  // full[2], empty[2], acc full, acc empty, bload[2]
+    uint32_t* tmem_slot = (uint32_t*)(bar + 8);
     S.abort_flag = (int*)(tmem_slot + 1);
     S.bbox = (float*)(S.abort_flag + 1);
     S.bbox_part = S.bbox + 6;
     S.nkeep = (unsigned char*)(S.bbox_part + 24);
-    S.bar_a = smem_u32(bar);
-    for (int i = tid; i < A_BYTES / 16; i += NTT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
+    S.bar_full = smem_u32(bar);
+    S.bar_empty = smem_u32(bar + 2);
+    S.bar_acc_full = smem_u32(bar + 4);
+    S.bar_acc_empty = smem_u32(bar + 5);
+    S.bar_bload = smem_u32(bar + 6);
+    for (int i = tid; i < NSTAGE * A_STAGE / 16; i += NTT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        mbar_init(S.bar_a, 1);
+        for (int s = 0; s < NSTAGE; ++s) {
+            mbar_init(S.bar_full + 8 * s, NTG);
+            mbar_init(S.bar_empty + 8 * s, 1);
+            mbar_init(S.bar_bload + 8 * s, 1);
+        }
+        mbar_init(S.bar_acc_full, 1);
+        mbar_init(S.bar_acc_empty, NTG);
         *S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -635,10 +734,10 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
 }
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
-constexpr size_t SMEM_BYTES =
-    1024 + A_BYTES + 3 * NMAX * 128 + 8 * MAX_CHUNKS + 8 + 8 + 4 * 6 + 4 * 24 + MAX_SHELLS + 64;
-static_assert(3 * 4 * 128 * 8 <= 3 * NMAX * 128, "epilogue partial sums must fit in the B operand buffer");
+constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * MAX_CHUNKS + 8 * 8 + 4 + 4 + 4 * 6 + 4 * 24 +
+                              MAX_SHELLS + 64;
 static_assert(SMEM_BYTES <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
+static_assert(KC == 32, "column masks are 32-bit and operand rows one 64-byte swizzle row");
 
 __device__ __forceinline__ void cta_teardown(const CtaState& S, uint32_t tm_cols)
 {
@@ -673,11 +772,11 @@ inline void tiling(const Grid& g, MolDesc& D)
 extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
 
 template <int NG>
-__global__ void __launch_bounds__(128 * NG, 1) rho_mixed_kernel(const Params P)
+__global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_kernel(const Params P)
 {
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t tm_cols = tmem_cols_for(P.npad);
-    CtaState S = cta_setup<128 * NG>(smem, tm_cols);
+    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, tm_cols);
     MolDesc D;
     D.B = P.B;
     D.g = P.g;
@@ -690,12 +789,13 @@ __global__ void __launch_bounds__(128 * NG, 1) rho_mixed_kernel(const Params P)
     D.tile0 = 0;
     D.npass = P.npass;
     D.npad = P.npad;
+    D.nmo = P.nmo;
     D.want_grad = P.want_grad;
     D.brick = P.brick;
     D.nby = P.nby;
     D.nbz = P.nbz;
     D.ntiles = P.ntiles;
-    uint32_t phase = 0;
+    Pipe pp;
     __shared__ long long next_tile;
     for (;;) {
         __syncthreads();
@@ -703,7 +803,7 @@ __global__ void __launch_bounds__(128 * NG, 1) rho_mixed_kernel(const Params P)
         __syncthreads();
         const long long tile = next_tile;
         if (tile >= P.ntiles || *S.abort_flag) break;
-        mixed_tile<NG>(D, tile, S, phase, P.status);
+        mixed_tile<NG>(D, tile, S, pp, P.status);
     }
     cta_teardown(S, tm_cols);
 }
@@ -722,15 +822,15 @@ struct BatchParams {
 };
 
 template <int NG>
-__global__ void __launch_bounds__(128 * NG, 1) rho_mixed_batch_kernel(const BatchParams P)
+__global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_batch_kernel(const BatchParams P)
 {
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    CtaState S = cta_setup<128 * NG>(smem, 512);
+    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, 512);
     __shared__ MolDesc Dsh;
     __shared__ long long work;
     __shared__ int cur_mol;
     if (threadIdx.x == 0) cur_mol = -1;
-    uint32_t phase = 0;
+    Pipe pp;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) work = (long long)atomicAdd(P.counter, (unsigned long long)P.grab);
@@ -752,15 +852,15 @@ __global__ void __launch_bounds__(128 * NG, 1) rho_mixed_batch_kernel(const Batc
                 }
             }
             __syncthreads();
-            mixed_tile<NG>(Dsh, t - Dsh.tile0, S, phase, P.status);
-            if (*S.abort_flag) break;
+            if (*S.abort_flag) break;  // read between two barriers: the same value in every thread
+            mixed_tile<NG>(Dsh, t - Dsh.tile0, S, pp, P.status);
         }
     }
     cta_teardown(S, 512);
 }
 
 // Split C_eff (nmo x ncart, FP64) into three BF16 parts in the B operand layout:
-// bpack[pass][chunk][part] is an npad x 64 K-major SWIZZLE_128B tile whose column
+// bpack[pass][chunk][part] is an npad x 32 K-major SWIZZLE_64B tile whose column
 // kk holds the coefficient of the listed Cartesian AO feeding mixed column kk.
 __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, const int* __restrict__ mcol_cart,
                               int nmchunk, int npass, int npad, __nv_bfloat16* __restrict__ bpack)
@@ -780,12 +880,11 @@ __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, 
         const __nv_bfloat16 h1 = __double2bfloat16(r1);
         const double r2 = r1 - (double)__bfloat162float(h1);
         const __nv_bfloat16 h2 = __double2bfloat16(r2);
-        const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((kk >> 3) ^ (n & 7)) & 7) << 4) +
-                                        ((kk & 7) << 1));
-        unsigned char* blk = (unsigned char*)bpack + ((long long)pass * nmchunk + c) * (3ll * npad * 128);
+        const uint32_t off = sw64_off(n, kk);
+        unsigned char* blk = (unsigned char*)bpack + ((long long)pass * nmchunk + c) * (3ll * npad * ROWB);
         *(__nv_bfloat16*)(blk + off) = h0;
-        *(__nv_bfloat16*)(blk + npad * 128 + off) = h1;
-        *(__nv_bfloat16*)(blk + 2 * npad * 128 + off) = h2;
+        *(__nv_bfloat16*)(blk + npad * ROWB + off) = h1;
+        *(__nv_bfloat16*)(blk + 2 * npad * ROWB + off) = h2;
     }
 }
 
@@ -832,21 +931,21 @@ static cudaError_t configure_kernels()
 static void launch_single(int ng, unsigned grid, cudaStream_t st, const Params& P)
 {
     if (ng == 3)
-        rho_mixed_kernel<3><<<grid, 384, SMEM_BYTES, st>>>(P);
+        rho_mixed_kernel<3><<<grid, 416, SMEM_BYTES, st>>>(P);
     else if (ng == 4)
-        rho_mixed_kernel<4><<<grid, 512, SMEM_BYTES, st>>>(P);
+        rho_mixed_kernel<4><<<grid, 544, SMEM_BYTES, st>>>(P);
     else
-        rho_mixed_kernel<2><<<grid, 256, SMEM_BYTES, st>>>(P);
+        rho_mixed_kernel<2><<<grid, 288, SMEM_BYTES, st>>>(P);
 }
 
 static void launch_batch(int ng, unsigned grid, cudaStream_t st, const BatchParams& P)
 {
     if (ng == 3)
-        rho_mixed_batch_kernel<3><<<grid, 384, SMEM_BYTES, st>>>(P);
+        rho_mixed_batch_kernel<3><<<grid, 416, SMEM_BYTES, st>>>(P);
     else if (ng == 4)
-        rho_mixed_batch_kernel<4><<<grid, 512, SMEM_BYTES, st>>>(P);
+        rho_mixed_batch_kernel<4><<<grid, 544, SMEM_BYTES, st>>>(P);
     else
-        rho_mixed_batch_kernel<2><<<grid, 256, SMEM_BYTES, st>>>(P);
+        rho_mixed_batch_kernel<2><<<grid, 288, SMEM_BYTES, st>>>(P);
 }
 }  // namespace mx
 }  // namespace okg
@@ -884,7 +983,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (major != 10 || minor != 3) return set_error(OKG_ERR_DEVICE, "okg_mixed_plan_create: needs an sm_103 GPU");
     if (b->dev.nshell > mx::MAX_SHELLS || b->dev.nmchunk > mx::MAX_CHUNKS)
-        return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: more than 2048 shells or 128 column chunks");
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: more than 2048 shells or 256 column chunks");
     okg_mixed_plan* p = (okg_mixed_plan*)calloc(1, sizeof(okg_mixed_plan));
     if (!p) return set_error(OKG_ERR_ALLOC, "okg_mixed_plan_create: host allocation");
     p->basis = b;
@@ -892,7 +991,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->npass = (nmo + n_max - 1) / n_max;
     const int per = (nmo + p->npass - 1) / p->npass;
     p->npad = (per + 15) / 16 * 16;
-    p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * 128;
+    p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * mx::ROWB;
     const size_t occ_off = (p->bpack_bytes + 255) & ~(size_t)255;
     const size_t st_off = occ_off + (((size_t)4 * p->npass * p->npad * 8 + 255) & ~(size_t)255);
     cudaError_t e = cudaMalloc(&p->block, st_off + 256);
@@ -972,6 +1071,7 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     P.occ = p->occ;
     P.npass = p->npass;
     P.npad = p->npad;
+    P.nmo = p->nmo;
     P.want_grad = want_grad;
     P.rho = d_rho;
     P.grad = d_grad;
@@ -1046,6 +1146,7 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
         D.tile0 = tile0;
         D.npass = p->npass;
         D.npad = p->npad;
+        D.nmo = p->nmo;
         D.want_grad = want_grad;
         tile0 += D.ntiles;
         sms = p->sm_count;
@@ -1224,11 +1325,11 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     const int npass = (nmo + NMAX - 1) / NMAX;
     const int per = (nmo + npass - 1) / npass;
     const int npad = (per + 15) / 16 * 16;
-    const size_t bpack_bytes = (size_t)npass * b->dev.nmchunk * 3 * npad * 128;
+    const size_t bpack_bytes = (size_t)npass * b->dev.nmchunk * 3 * npad * ROWB;
     const size_t occ_off = (bpack_bytes + 255) & ~(size_t)255;
     const size_t st_off = occ_off + (((size_t)4 * npass * npad * 8 + 255) & ~(size_t)255);
     if (b->dev.nshell > MAX_SHELLS || b->dev.nmchunk > MAX_CHUNKS)
-        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: more than 2048 shells or 128 column chunks");
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: more than 2048 shells or 256 column chunks");
     if (st_off + 256 > NOALLOC_SCRATCH_BYTES)
         return set_error(OKG_ERR_UNSUPPORTED,
                          "okg_rho_mixed_noalloc: this basis and MO count need more than the 2 MiB of static "
@@ -1274,6 +1375,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     P.occ = occ;
     P.npass = npass;
     P.npad = npad;
+    P.nmo = nmo;
     P.want_grad = want_grad;
     P.rho = d_rho;
     P.grad = d_grad;
