@@ -261,6 +261,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     // mixed-path chunks: whole shells, canonical columns, at most OKG_MKC per chunk
     std::vector<int4> mchunks;
     std::vector<int> mcol_cart;
+    std::vector<double> mcol_g;  // angular norm of each column (folded into the MO coefficients)
     {
         int s0 = 0, col = 0;
         for (int s = 0; s <= nshell; ++s) {
@@ -269,10 +270,14 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
                 mchunks.push_back(make_int4(s0, s, col, 0));
                 const size_t base = mcol_cart.size();
                 mcol_cart.resize(base + OKG_MKC, -1);
+                mcol_g.resize(base + OKG_MKC, 0.0);
                 for (int t = s0; t < s; ++t)
                     for (int q = 0; q < ncanon(shells[t].L); ++q) {
                         const int r = comp_row[shells[t].comp0 + q];
-                        if (r >= 0) mcol_cart[base + shells[t].mcol + q] = shells[t].cart0 + r;
+                        if (r >= 0) {
+                            mcol_cart[base + shells[t].mcol + q] = shells[t].cart0 + r;
+                            mcol_g[base + shells[t].mcol + q] = comp_g[shells[t].comp0 + q];
+                        }
                     }
                 s0 = s;
                 col = 0;
@@ -284,7 +289,6 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
             }
         }
     }
-    std::vector<float> comp_g32(comp_g.begin(), comp_g.end());
 
     okg_basis* b = (okg_basis*)calloc(1, sizeof(okg_basis));
     if (!b) return set_error(OKG_ERR_ALLOC, "okg_basis_create: host allocation");
@@ -302,9 +306,9 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     const size_t o_chunks = lay.take(sizeof(int4) * chunks.size());
     const size_t o_pmx = lay.take(sizeof(PrimMx) * nprim);
     const size_t o_padj = lay.take(sizeof(double) * 2 * nprim);
-    const size_t o_cg32 = lay.take(sizeof(float) * comp_g32.size());
     const size_t o_mch = lay.take(sizeof(int4) * mchunks.size());
     const size_t o_mcc = lay.take(sizeof(int) * mcol_cart.size());
+    const size_t o_mcg = lay.take(sizeof(double) * mcol_g.size());
     const size_t bytes = lay.take(0);
     char* blk = nullptr;
     cudaError_t e = cudaMalloc((void**)&blk, bytes);
@@ -328,11 +332,11 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-        e = cudaMemcpy(blk + o_cg32, comp_g32.data(), sizeof(float) * comp_g32.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_mch, mchunks.data(), sizeof(int4) * mchunks.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_mcc, mcol_cart.data(), sizeof(int) * mcol_cart.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(blk + o_mcg, mcol_g.data(), sizeof(double) * mcol_g.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(blk);
         free(b);
@@ -353,9 +357,9 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     d.chunks = (const int4*)(blk + o_chunks);
     d.prim_mx = (const PrimMx*)(blk + o_pmx);
     d.prim_adj = (const double*)(blk + o_padj);
-    d.comp_g32 = (const float*)(blk + o_cg32);
     d.mchunks = (const int4*)(blk + o_mch);
     d.mcol_cart = (const int*)(blk + o_mcc);
+    d.mcol_g = (const double*)(blk + o_mcg);
     d.nmchunk = (int)mchunks.size();
     d.natom = natom;
     d.nshell = nshell;

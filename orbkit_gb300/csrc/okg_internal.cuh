@@ -75,9 +75,9 @@ struct BasisDev {
     const int4* chunks;      // nchunk x {first shell, end shell, first Cartesian row, end row}
     const PrimMx* prim_mx;   // nprim (mixed path)
     const double* prim_adj;  // nprim x 2 : dw/dalpha, w/c (the alpha-dependent norm) for the adjoint
-    const float* comp_g32;   // comp_g in FP32 (mixed path)
     const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= OKG_MKC columns)
     const int* mcol_cart;    // nmchunk x OKG_MKC: listed Cartesian row feeding each column, or -1
+    const double* mcol_g;    // nmchunk x OKG_MKC: angular norm of each column (0 where unused)
     int natom, nshell, nprim, ncart, nsph, spherical;
     int max_nprim, nchunk, nmchunk;
 };

@@ -41,6 +41,7 @@
 //     component) of its 32 points.
 // Every wait is bounded and raises the status word instead of hanging.
 #include <stdio.h>
+#include <string.h>
 
 #include <cuda_bf16.h>
 
@@ -55,29 +56,13 @@ constexpr int M = 128;
 constexpr int KC = OKG_MKC;           // 32 BF16 = 64 bytes
 constexpr int ROWB = KC * 2;          // bytes of one operand row
 constexpr int RUNITS = ROWB / 16;     // 16-byte units of one operand row
-constexpr int NG_DEFAULT = 4;         // generation groups per point (generation threads = 128 x groups)
+constexpr int NG_DEFAULT = 3;         // generation groups per point (generation threads = 128 x groups)
 constexpr int A_TILE = M * ROWB;      // bytes of one 128 x 32 BF16 sub-tile
 constexpr int A_STAGE = 12 * A_TILE;  // 4 channels x 3 parts
 constexpr int NMAX = 64;              // MO columns per pass
 constexpr int B_STAGE = 3 * NMAX * ROWB;
 constexpr int NSTAGE = 2;
 constexpr long long WAIT_LIMIT = 1ll << 24;
-
-struct Params {
-    BasisDev B;
-    Grid g;
-    const uint4* bpack;    // [npass][nmchunk][3][npad x 64 B], pre-swizzled
-    const double* occ;     // [npass * npad], zero padded
-    int npass, npad, nmo;
-    int want_grad;
-    double* rho;
-    double* grad;          // 3 x ld
-    long long ld;
-    int* status;           // device status word: 1 = timeout
-    long long ntiles;
-    int brick, nby, nbz;   // tiling (see tiling())
-    unsigned long long* counter;  // tile counter, zero at launch (tiles are handed out dynamically)
-};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
 {
@@ -238,7 +223,7 @@ __host__ __device__ __forceinline__ uint32_t sw64_off(int m, int k)
 }
 
 // One molecule as seen by a tile: its basis tables, grid, coefficient tiles and outputs.
-struct MolDesc {
+struct alignas(16) MolDesc {
     BasisDev B;
     Grid g;
     const uint4* bpack;  // [npass][nmchunk][3][npad x 64 B], pre-swizzled
@@ -256,33 +241,39 @@ struct MolDesc {
     int nby, nbz;        // bricks along y and z
 };
 
+// Single-molecule launch.
+struct Params {
+    MolDesc D;
+    int* status;                  // device status word: 1 = timeout
+    unsigned long long* counter;  // tile counter, zero at launch (tiles are handed out dynamically)
+};
+
 // Screening: a primitive is skipped for a tile when alpha log2(e) d^2 > SCREEN_LOG2,
 // d = distance from its atom to the tile's bounding box, i.e. its exponential is
 // below 2^-64 (5e-20) at every point of the tile.
 constexpr float SCREEN_LOG2 = 64.0f;
 
-// Shared-memory pieces of the CTA used by every tile.
+// Shared-memory pieces of the CTA.  Two tile buffers (tile index, column masks,
+// batch descriptor) let the generation threads screen the next tile while the
+// MMA warp still works through the previous one.
 struct CtaState {
     unsigned char* A_s;          // NSTAGE x A_STAGE
     unsigned char* B_s;          // NSTAGE x B_STAGE
     uint32_t bar_full;           // NSTAGE mbarriers, 8 B apart: stage written by every generation thread
     uint32_t bar_empty;          // NSTAGE mbarriers: the stage's MMAs are complete (tcgen05.commit)
     uint32_t bar_bload;          // NSTAGE mbarriers: the stage's B block has landed (bulk copy)
-    uint32_t bar_acc_full;       // accumulators of an MO pass complete (tcgen05.commit)
+    uint32_t bar_acc_full;       // accumulators of a job (tile, MO pass) complete (tcgen05.commit)
     uint32_t bar_acc_empty;      // every generation thread has read the accumulators
+    uint32_t bar_screened;       // 2 mbarriers (tile buffers): tile index and column masks written
+    uint32_t bar_kfree;          // 2 mbarriers: the MMA warp is done with the buffer's tile
     uint32_t tmem;
     int* abort_flag;
-    float* bbox;                 // lo x,y,z, hi x,y,z of the current tile
+    float* bbox;                 // lo x,y,z, hi x,y,z of the tile being screened
     float* bbox_part;            // 4 warps x 6
-    unsigned char* nkeep;        // per shell: primitives kept for the current tile
-    unsigned* kmask;             // per chunk: columns whose shell is kept for the current tile
-};
-
-// Position in the CTA's stream of chunks and MO passes; the generation threads and
-// the MMA warp each keep a copy and advance it identically.
-struct Pipe {
-    uint32_t seq = 0;  // chunks issued so far (stage = seq % 2, use = seq / 2)
-    uint32_t acc = 0;  // MO passes whose accumulators were handed over so far
+    unsigned char* nkeep;        // per shell: primitives kept for the tile being generated
+    unsigned* kmask;             // 2 x MAX_CHUNKS: per chunk, columns whose shell is kept for the buffer's tile
+    long long* tile_slot;        // 2: tile of the buffer (local to its molecule); -1: no more tiles
+    MolDesc* mol;                // 2: molecule of the buffer's tile (one copy for the single-molecule kernel)
 };
 
 // Per-tile screening tables live in shared memory: at most MAX_SHELLS shells and
@@ -370,270 +361,94 @@ __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int
     return true;
 }
 
-// Generation side of one tile (threads 0 .. 128 NG - 1): per MO pass and kept
-// chunk, the AO values of this thread's atoms at its point into a free stage; per
-// pass the epilogue over this warp's outputs; at the end the stores.
-template <int NG>
-__device__ __forceinline__ void gen_tile(const MolDesc& D, const CtaState& S, Pipe& pp, int* status, bool valid,
-                                         long long p, double x, double y, double z)
+// Generation threads only: a named barrier (id 1) over the 128 NG generation threads.
+template <int NTG>
+__device__ __forceinline__ void gen_sync()
 {
-    const int tid = threadIdx.x;
-    const int warp = tid >> 5;
-    const int lane = tid & 31;
-    const int prow = tid & (M - 1);  // point row of this thread in the tile
-    const int grp = tid >> 7;        // generation group: atom runs of a pass go round-robin to the NG groups
-    const BasisDev& B = D.B;
-    const int npad = D.npad;
-    const unsigned chmask = D.want_grad ? 0xFu : 0x1u;
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its 32 points = rows prow) and
-    // owns the outputs o (0 = rho, 1..3 = d/dx, d/dy, d/dz) with o % NG == w / 4
-    const int q = warp & 3, h = warp >> 2;
-    bool own[4];
-#pragma unroll
-    for (int o = 0; o < 4; ++o) own[o] = (o % NG == h) && (o == 0 || D.want_grad);
-    const bool any_own = own[0] || own[1] || own[2] || own[3];
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-
-    for (int pass = 0; pass < D.npass; ++pass) {
-        int nchunks = 0;
-        int last_atom = -1, ord = -1;
-        bool mine = false;
-        double rr = 0;
-        float Xf = 0, Yf = 0, Zf = 0;
-        for (int c = 0; c < B.nmchunk; ++c) {
-            if (S.kmask[c] == 0u) continue;  // nothing of this chunk reaches the tile
-            const uint32_t s = pp.seq & 1u, u = pp.seq >> 1;
-            unsigned char* A_s = S.A_s + s * A_STAGE;
-            if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
-            const int4 ck = B.mchunks[c];
-            for (int si = ck.x; si < ck.y; ++si) {
-                const Shell sh = load_shell(B.shells + si);
-                if (sh.atom != last_atom) {
-                    last_atom = sh.atom;
-                    ++ord;
-                    mine = ord % NG == grp;
-                    if (mine) {
-                        const double X = x - B.atoms[4 * sh.atom];
-                        const double Y = y - B.atoms[4 * sh.atom + 1];
-                        const double Z = z - B.atoms[4 * sh.atom + 2];
-                        rr = X * X + Y * Y + Z * Z;
-                        Xf = dbl_to_flt_rn(X);
-                        Yf = dbl_to_flt_rn(Y);
-                        Zf = dbl_to_flt_rn(Z);
-                    }
-                }
-                if (!mine) continue;
-                const int nk = S.nkeep[si];
-                if (nk == 0) continue;
-                float R0 = 0.f, R1 = 0.f;
-                for (int k = 0; k < nk; ++k) {
-                    const PrimMx pm = B.prim_mx[sh.prim0 + k];
-                    const float e = exp2_neg(pm.a2 * rr);
-                    R0 = fmaf(pm.w, e, R0);
-                    R1 = fmaf(pm.wa, e, R1);
-                }
-                const Radial<float> r{R0, R1, 0.f};
-                shell_eval_L(sh.L, Xf, Yf, Zf, r, chmask, false, [&](int ch, int j, float v) {
-                    v *= B.comp_g32[sh.comp0 + j];
-                    __nv_bfloat16 b0, b1, b2;
-                    split3(v, b0, b1, b2);
-                    unsigned char* base = A_s + ch * 3 * A_TILE + sw64_off(prow, sh.mcol + j);
-                    *(__nv_bfloat16*)(base) = b0;
-                    *(__nv_bfloat16*)(base + A_TILE) = b1;
-                    *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
-                });
-            }
-            fence_proxy_async();
-            mbar_arrive(S.bar_full + 8 * s);
-            ++pp.seq;
-            ++nchunks;
-        }
-        if (nchunks == 0) continue;  // no AO of any chunk reaches this tile: this pass contributes zero
-        const uint32_t P = pp.acc++;
-        if (!mbar_wait(S.bar_acc_full, P & 1u, status)) *S.abort_flag = 1;
-        tc_fence_after();
-        if (any_own) {
-            const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
-            const float2* occf = D.occf + pass * npad;
-            const float2* occ2f = D.occf + (D.npass + pass) * npad;
-            const int nlead = 2 * nchunks < 4 ? 2 * nchunks : 4;  // leading accumulators written in this pass
-            int mo_end = D.nmo - pass * npad;
-            mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
-            for (int m0 = 0; m0 < mo_end; m0 += 8) {
-                float v[8], a1[8], a2[8], a3[8], lo[8];
-                tmem_ld8(tl + 0 * npad + m0, v);
-                tmem_ld8(tl + 1 * npad + m0, a1);
-                tmem_ld8(tl + 2 * npad + m0, a2);
-                tmem_ld8(tl + 3 * npad + m0, a3);
-                tmem_ld8(tl + 4 * npad + m0, lo);
-                tmem_wait_ld();
-                if (nlead < 4) {
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        a2[i] = nlead > 2 ? a2[i] : 0.f;
-                        a3[i] = 0.f;
-                    }
-                }
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[i] = ((v[i] + a1[i]) + (a2[i] + a3[i])) + lo[i];
-                // sum_i occ_i v_i^2 and sum_i 2 occ_i v_i vd_i over the 8 MOs in double-float
-                // FP32 arithmetic (exact products by FMA, two-sum accumulation, about 44
-                // bits), then the group sums are added to the FP64 accumulators
-                if (own[0]) {
-                    DF sr;
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) sr.add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
-                    acc[0] += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
-                }
-#pragma unroll
-                for (int o = 1; o < 4; ++o) {
-                    if (!own[o]) continue;
-                    float vd[8];
-                    tmem_ld8(tl + (4 + o) * npad + m0, vd);
-                    tmem_wait_ld();
-                    DF sd;
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
-                    acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
-                }
-            }
-        }
-        tc_fence_before();
-        mbar_arrive(S.bar_acc_empty);
-    }
-    (void)lane;
-    if (valid && !*S.abort_flag) {
-        if (own[0]) D.rho[p] = acc[0];
-#pragma unroll
-        for (int o = 1; o < 4; ++o)
-            if (own[o]) D.grad[(long long)(o - 1) * D.ld + p] = acc[o];
-    }
+    asm volatile("bar.sync 1, %0;" ::"r"(NTG) : "memory");
 }
 
-// MMA side of one tile (the last warp): per MO pass and kept chunk, the masked B
-// copy into the stage, then 48 MMAs (or 12 without gradient) from lane 0 once the
-// generation threads filled the stage.
-__device__ __forceinline__ void mma_tile(const MolDesc& D, const CtaState& S, Pipe& pp, int* status)
+// Next chunk after c (in chunk order) with a kept column, or -1.
+__device__ __forceinline__ int next_kept(const unsigned* km, int nmchunk, int c)
 {
-    const int lane = threadIdx.x & 31;
-    const BasisDev& B = D.B;
-    const int npad = D.npad;
-    const uint32_t idesc = idesc_bf16(M, npad);
-    const int bunits = 3 * npad * RUNITS;  // 16-byte units of one B block
-    const int nch = D.want_grad ? 4 : 1;
-    const uint32_t bpart16 = (uint32_t)(npad * ROWB) >> 4;
-    for (int pass = 0; pass < D.npass; ++pass) {
-        int kq = 0;  // K-steps issued in this pass
-        for (int c = 0; c < B.nmchunk; ++c) {
-            const unsigned km = S.kmask[c];
-            if (km == 0u) continue;
-            const uint32_t s = pp.seq & 1u, u = pp.seq >> 1;
-            unsigned char* B_s = S.B_s + s * B_STAGE;
-            // B block of this (pass, chunk) by one bulk copy once the stage is free
-            if (lane == 0) {
-                if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
-                bulk_load(smem_u32(B_s), D.bpack + ((long long)pass * B.nmchunk + c) * bunits, (uint32_t)bunits * 16u,
-                          S.bar_bload + 8 * s);
-            }
-            __syncwarp();
-            if (!mbar_wait(S.bar_bload + 8 * s, u & 1u, status)) *S.abort_flag = 1;
-            // columns of screened shells are zeroed.  Lane l touches the 16-byte units
-            // l, l + 32, ...: rows n = l / 4 (mod 8) of every part, physical unit l % 4, so
-            // with rows of 4 units and the 64-byte swizzle (unit ^ (n >> 1) % 4) always the
-            // same logical 8-column group
-            const unsigned m8 = (km >> (8 * ((lane & 3) ^ ((lane >> 3) & 3)))) & 0xFFu;
-            if (m8 != 0xFFu) {
-                unsigned keep[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    keep[t] = ((m8 >> (2 * t)) & 1u ? 0x0000FFFFu : 0u) | ((m8 >> (2 * t + 1)) & 1u ? 0xFFFF0000u : 0u);
-                for (int i = lane; i < bunits; i += 32) {
-                    const uint4 v = ((const uint4*)B_s)[i];
-                    ((uint4*)B_s)[i] = make_uint4(v.x & keep[0], v.y & keep[1], v.z & keep[2], v.w & keep[3]);
-                }
-                fence_proxy_async();
-            }
-            __syncwarp();
-            if (lane == 0) {
-                // the previous pass's accumulators must have been read before they are overwritten
-                if (kq == 0 && pp.acc > 0 && !mbar_wait(S.bar_acc_empty, (pp.acc - 1) & 1u, status))
-                    *S.abort_flag = 1;
-                if (!mbar_wait(S.bar_full + 8 * s, u & 1u, status)) *S.abort_flag = 1;
-                tc_fence_after();
-                if (!*S.abort_flag) {
-                    // descriptors differ only in the start-address field (bytes >> 4)
-                    const uint64_t adesc = sdesc(smem_u32(S.A_s + s * A_STAGE)), bdesc = sdesc(smem_u32(B_s));
-#pragma unroll 1
-                    for (int ch = 0; ch < nch; ++ch) {
-#pragma unroll
-                        for (int k = 0; k < KC / 16; ++k) {
-                            const int ks = kq + k;
-                            // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
-                            const int pa[6] = {0, 0, 1, 0, 1, 2};
-                            const int pb[6] = {0, 1, 0, 2, 1, 0};
-#pragma unroll
-                            for (int t = 0; t < 6; ++t) {
-                                const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 32) >> 4);
-                                const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
-                                uint32_t col, accf;
-                                if (ch == 0 && t == 0) {  // leading product -> accumulator ks mod 4
-                                    col = ks & 3;
-                                    accf = ks >= 4;
-                                } else if (ch == 0) {     // value corrections -> accumulator 4
-                                    col = 4;
-                                    accf = ks > 0 || t > 1;
-                                } else {                  // gradient channel ch -> accumulator 4 + ch
-                                    col = 4 + ch;
-                                    accf = ks > 0 || t > 0;
-                                }
-                                mma_bf16(S.tmem + col * npad, ad, bd, idesc, accf);
-                            }
-                        }
-                    }
-                    mma_commit(S.bar_empty + 8 * s);
-                } else {
-                    mbar_arrive(S.bar_empty + 8 * s);
-                }
-            }
-            __syncwarp();
-            ++pp.seq;
-            kq += KC / 16;
-        }
-        if (kq > 0) {
-            if (lane == 0) {
-                if (!*S.abort_flag)
-                    mma_commit(S.bar_acc_full);
-                else
-                    mbar_arrive(S.bar_acc_full);
-            }
-            __syncwarp();
-            ++pp.acc;
-        }
-    }
+    for (++c; c < nmchunk; ++c)
+        if (km[c] != 0u) return c;
+    return -1;
 }
 
-// One 128-point tile of one molecule (every thread of the CTA): bounding box and
-// screening of every shell against it, then the generation threads and the MMA
-// warp each run their side.
-template <int NG>
-__device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, const CtaState& S, Pipe& pp,
-                                           int* status)
-{
-    constexpr int NTG = 128 * NG;  // generation threads
-    const int tid = threadIdx.x;
-    const int warp = tid >> 5;
-    const int lane = tid & 31;
-    const bool gen = tid < NTG;
-    const int prow = tid & (M - 1);
-    const BasisDev& B = D.B;
+// Where the tiles come from: a device counter over one molecule's tiles, or grabs
+// of consecutive tiles of a batch (molecule found by binary search over tile0).
+struct TileFeed {
+    unsigned long long* counter;  // zero at launch
+    long long ntiles;             // tiles of the molecule, or of the whole batch
+    const MolDesc* descs;         // batch: nmol descriptors, ascending tile0
+    int nmol, grab;
+};
 
-    long long p = 0;
-    bool valid = false;
-    double x = 0, y = 0, z = 0;
-    if (gen) {
-        valid = tile_point(D, tile, prow, p);
-        grid_point(D.g, p, x, y, z);
+// Generation threads: take the next tile into buffer `ord` % 2 (once the MMA warp
+// has released the buffer's previous tile), this thread's point of it, the tile's
+// bounding box and the screening of every shell against it; then each thread
+// arrives on the buffer's "screened" barrier.  Returns the tile (local to its
+// molecule) or -1 when there are no more.
+template <int NG, bool BATCH>
+__device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const CtaState& S, uint32_t ord,
+                                                      long long& gnext, long long& gend, long long& p, bool& valid,
+                                                      double& x, double& y, double& z, int* status)
+{
+    constexpr int NTG = 128 * NG;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int b = ord & 1;
+    if (ord >= 2 && !mbar_wait(S.bar_kfree + 8 * b, ((ord >> 1) - 1) & 1u, status)) *S.abort_flag = 1;
+    // every generation thread is done with the buffer's previous tile (its epilogue
+    // and stores read the buffer's descriptor) before warp 0 overwrites it
+    gen_sync<NTG>();
+    if (warp == 0) {
+        long long t = -1;
+        int mol = 0;
+        if (lane == 0 && !*S.abort_flag) {
+            if (!BATCH) {
+                t = (long long)atomicAdd(F.counter, 1ull);
+                if (t >= F.ntiles) t = -1;
+            } else {
+                if (gnext >= gend) {
+                    gnext = (long long)atomicAdd(F.counter, (unsigned long long)F.grab);
+                    gend = gnext + F.grab < F.ntiles ? gnext + F.grab : F.ntiles;
+                }
+                if (gnext < gend) {
+                    t = gnext++;
+                    int lo = 0, hi = F.nmol - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (F.descs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+                    }
+                    mol = lo;
+                }
+            }
+        }
+        if (BATCH) {
+            t = __shfl_sync(0xffffffffu, t, 0);
+            mol = __shfl_sync(0xffffffffu, mol, 0);
+            if (t >= 0) {
+                constexpr int U = (int)(sizeof(MolDesc) / 16);
+                const uint4* src = (const uint4*)(F.descs + mol);
+                uint4* dst = (uint4*)(S.mol + b);
+                for (int i = lane; i < U; i += 32) dst[i] = src[i];
+                if (lane == 0) t -= F.descs[mol].tile0;
+            }
+        }
+        if (lane == 0) S.tile_slot[b] = t;
     }
+    gen_sync<NTG>();
+    const long long tile = S.tile_slot[b];
+    if (tile < 0) {
+        mbar_arrive(S.bar_screened + 8 * b);
+        return -1;
+    }
+    const MolDesc& D = S.mol[BATCH ? b : 0];
+    const BasisDev& B = D.B;
+    valid = tile_point(D, tile, tid & (M - 1), p);
+    grid_point(D.g, p, x, y, z);
+    unsigned* km = S.kmask + b * MAX_CHUNKS;
     // bounding box of the tile's valid points (rows 0..127 = warps 0..3)
     if (warp < 4) {
         float v[6];
@@ -653,61 +468,460 @@ __device__ __forceinline__ void mixed_tile(const MolDesc& D, long long tile, con
         if (lane == 0)
             for (int c = 0; c < 6; ++c) S.bbox_part[warp * 6 + c] = v[c];
     }
-    __syncthreads();
+    for (int c = tid; c < B.nmchunk; c += NTG) km[c] = 0u;
+    gen_sync<NTG>();
     if (tid < 6) {
         float a = S.bbox_part[tid];
         for (int w = 1; w < 4; ++w)
             a = tid < 3 ? fminf(a, S.bbox_part[w * 6 + tid]) : fmaxf(a, S.bbox_part[w * 6 + tid]);
         S.bbox[tid] = a;
     }
-    if (gen)
-        for (int c = tid; c < B.nmchunk; c += NTG) S.kmask[c] = 0u;
-    __syncthreads();
-    // screening of every shell against the tile's bounding box, once per tile
-    if (gen) {
-        for (int si = tid; si < B.nshell; si += NTG) {
-            const Shell sh = load_shell(B.shells + si);
-            const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
-                        az = (float)B.atoms[4 * sh.atom + 2];
-            const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
-            const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
-            const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            int nk = 0;
-            while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
-            S.nkeep[si] = (unsigned char)nk;
-            if (nk > 0) atomicOr(S.kmask + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
+    gen_sync<NTG>();
+    // a primitive is kept while alpha log2(e) d^2 <= SCREEN_LOG2 (primitives sorted by alpha per shell)
+    for (int si = tid; si < B.nshell; si += NTG) {
+        const Shell sh = load_shell(B.shells + si);
+        const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
+                    az = (float)B.atoms[4 * sh.atom + 2];
+        const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
+        const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
+        const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        int nk = 0;
+        while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+        S.nkeep[si] = (unsigned char)nk;
+        if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
+    }
+    gen_sync<NTG>();
+    mbar_arrive(S.bar_screened + 8 * b);
+    return tile;
+}
+
+// Atoms of a job go round-robin to the generation groups in the order of the
+// job's shells; the group owning an atom keeps its r^2 and coordinates.
+struct AtomRun {
+    int last_atom = -1, ord = -1;
+    bool mine = false;
+    double rr = 0;
+    float X = 0, Y = 0, Z = 0;
+};
+
+// Generation threads: the AO values (4 or 1 channels x 3 BF16 parts) of one kept
+// chunk for this thread's point and atoms, into the next stage of the ring.
+template <int NG>
+__device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaState& S, uint32_t& seq, AtomRun& ar,
+                                          unsigned chmask, double x, double y, double z, int* status)
+{
+    const int tid = threadIdx.x;
+    const int prow = tid & (M - 1);  // point row of this thread in the tile
+    const int grp = tid >> 7;        // generation group
+    const uint32_t s = seq & 1u, u = seq >> 1;
+    unsigned char* A_s = S.A_s + s * A_STAGE;
+    if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
+    const int4 ck = B.mchunks[c];
+    Shell nx = load_shell(B.shells + ck.x);  // records are loaded one shell ahead
+    for (int si = ck.x; si < ck.y; ++si) {
+        const Shell sh = nx;
+        if (si + 1 < ck.y) nx = load_shell(B.shells + si + 1);
+        if (sh.atom != ar.last_atom) {
+            ar.last_atom = sh.atom;
+            ++ar.ord;
+            ar.mine = ar.ord % NG == grp;
+            if (ar.mine) {
+                const double X = x - B.atoms[4 * sh.atom];
+                const double Y = y - B.atoms[4 * sh.atom + 1];
+                const double Z = z - B.atoms[4 * sh.atom + 2];
+                ar.rr = X * X + Y * Y + Z * Z;
+                ar.X = dbl_to_flt_rn(X);
+                ar.Y = dbl_to_flt_rn(Y);
+                ar.Z = dbl_to_flt_rn(Z);
+            }
+        }
+        if (!ar.mine) continue;
+        const int nk = S.nkeep[si];
+        if (nk == 0) continue;
+        // primitives two at a time (two independent exponentials in flight)
+        float R0 = 0.f, R1 = 0.f;
+        for (int k = 0; k < nk; k += 2) {
+            const PrimMx pa = B.prim_mx[sh.prim0 + k];
+            const float ea = exp2_neg(pa.a2 * ar.rr);
+            if (k + 1 < nk) {
+                const PrimMx pb = B.prim_mx[sh.prim0 + k + 1];
+                const float eb = exp2_neg(pb.a2 * ar.rr);
+                R0 = fmaf(pb.w, eb, R0);
+                R1 = fmaf(pb.wa, eb, R1);
+            }
+            R0 = fmaf(pa.w, ea, R0);
+            R1 = fmaf(pa.wa, ea, R1);
+        }
+        const Radial<float> r{R0, R1, 0.f};
+        shell_eval_L(sh.L, ar.X, ar.Y, ar.Z, r, chmask, false, [&](int ch, int j, float v) {
+            __nv_bfloat16 b0, b1, b2;
+            split3(v, b0, b1, b2);
+            unsigned char* base = A_s + ch * 3 * A_TILE + sw64_off(prow, sh.mcol + j);
+            *(__nv_bfloat16*)(base) = b0;
+            *(__nv_bfloat16*)(base + A_TILE) = b1;
+            *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
+        });
+    }
+    fence_proxy_async();
+    mbar_arrive(S.bar_full + 8 * s);
+    ++seq;
+}
+
+// Generation threads: the epilogue of one job.  Warp w reads TMEM lanes
+// 32 (w % 4) .. (its 32 points) and owns the outputs o (0 = rho, 1..3 = d/dx,
+// d/dy, d/dz) with o % NG == w / 4; the 8-MO groups are reduced in double-float
+// FP32 (exact products by FMA, two-sum accumulation, about 44 bits) and added to
+// the FP64 accumulators.
+template <int NG>
+__device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nchunks, const CtaState& S,
+                                             uint32_t& accseq, double (&acc)[4], int* status)
+{
+    const int warp = threadIdx.x >> 5;
+    const int q = warp & 3, h = warp >> 2;
+    const int npad = D.npad;
+    bool own[4];
+#pragma unroll
+    for (int o = 0; o < 4; ++o) own[o] = (o % NG == h) && (o == 0 || D.want_grad);
+    if (!mbar_wait(S.bar_acc_full, accseq & 1u, status)) *S.abort_flag = 1;
+    ++accseq;
+    tc_fence_after();
+    if (own[0] || own[1] || own[2] || own[3]) {
+        const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
+        const float2* occf = D.occf + pass * npad;
+        const float2* occ2f = D.occf + (D.npass + pass) * npad;
+        const int nlead = 2 * nchunks < 4 ? 2 * nchunks : 4;  // leading accumulators written in this job
+        int mo_end = D.nmo - pass * npad;
+        mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
+        for (int m0 = 0; m0 < mo_end; m0 += 8) {
+            float v[8], a1[8], a2[8], a3[8], lo[8];
+            tmem_ld8(tl + 0 * npad + m0, v);
+            tmem_ld8(tl + 1 * npad + m0, a1);
+            tmem_ld8(tl + 2 * npad + m0, a2);
+            tmem_ld8(tl + 3 * npad + m0, a3);
+            tmem_ld8(tl + 4 * npad + m0, lo);
+            tmem_wait_ld();
+            if (nlead < 4) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    a2[i] = nlead > 2 ? a2[i] : 0.f;
+                    a3[i] = 0.f;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = ((v[i] + a1[i]) + (a2[i] + a3[i])) + lo[i];
+            if (own[0]) {
+                DF sr;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) sr.add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
+                acc[0] += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
+            }
+#pragma unroll
+            for (int o = 1; o < 4; ++o) {
+                if (!own[o]) continue;
+                float vd[8];
+                tmem_ld8(tl + (4 + o) * npad + m0, vd);
+                tmem_wait_ld();
+                DF sd;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
+                acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
+            }
         }
     }
-    __syncthreads();
-    if (gen)
-        gen_tile<NG>(D, S, pp, status, valid, p, x, y, z);
-    else
-        mma_tile(D, S, pp, status);
+    tc_fence_before();
+    mbar_arrive(S.bar_acc_empty);
+}
+
+// Generation side of the CTA.  Jobs (tile, MO pass) are generated in order; the
+// first chunk of the next job (screening its tile first when it starts one) is
+// generated before the epilogue of the current job, so the tensor core's tail
+// of a job overlaps useful work.
+template <int NG, bool BATCH>
+__device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, int* status)
+{
+    const int warp = threadIdx.x >> 5;
+    const int h = warp >> 2;
+    uint32_t seq = 0, accseq = 0, ord = 0;
+    long long gnext = 0, gend = 0;
+    long long p = 0;
+    bool valid = false;
+    double x = 0, y = 0, z = 0;
+    if (fetch_and_screen<NG, BATCH>(F, S, ord, gnext, gend, p, valid, x, y, z, status) < 0) return;
+    int gpass = 0;
+    AtomRun ar;
+    int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
+    int nch = 0;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (;;) {
+        const MolDesc& Dg = S.mol[BATCH ? (ord & 1) : 0];
+        const unsigned* km = S.kmask + (ord & 1) * MAX_CHUNKS;
+        {
+            const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
+            const BasisDev& B = Dg.B;
+            while (c >= 0) {
+                gen_chunk<NG>(B, c, S, seq, ar, chmask, x, y, z, status);
+                ++nch;
+                c = next_kept(km, B.nmchunk, c);
+            }
+        }
+        // the next job: the next MO pass of this tile, or pass 0 of a new tile
+        int npass_next = gpass + 1;
+        uint32_t ord_next = ord;
+        long long p_next = p;
+        bool valid_next = valid, more = true;
+        if (npass_next == Dg.npass) {
+            ord_next = ord + 1;
+            npass_next = 0;
+            more = fetch_and_screen<NG, BATCH>(F, S, ord_next, gnext, gend, p_next, valid_next, x, y, z, status) >= 0;
+        }
+        int c_next = -1, nch_next = 0;
+        if (more) {
+            const MolDesc& Dn = S.mol[BATCH ? (ord_next & 1) : 0];
+            const unsigned* kmn = S.kmask + (ord_next & 1) * MAX_CHUNKS;
+            ar = AtomRun();
+            c_next = next_kept(kmn, Dn.B.nmchunk, -1);
+            if (c_next >= 0) {
+                gen_chunk<NG>(Dn.B, c_next, S, seq, ar, Dn.want_grad ? 0xFu : 0x1u, x, y, z, status);
+                ++nch_next;
+                c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
+            }
+        }
+        // the current job's epilogue (nothing to read if none of its chunks reached the tile)
+        if (nch > 0) gen_epilogue<NG>(Dg, gpass, nch, S, accseq, acc, status);
+        if (gpass == Dg.npass - 1) {
+            if (valid && !*S.abort_flag) {
+                if (0 % NG == h) Dg.rho[p] = acc[0];
+                if (Dg.want_grad) {
+#pragma unroll
+                    for (int o = 1; o < 4; ++o)
+                        if (o % NG == h) Dg.grad[(long long)(o - 1) * Dg.ld + p] = acc[o];
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 4; ++o) acc[o] = 0.0;
+        }
+        if (!more) break;
+        gpass = npass_next;
+        ord = ord_next;
+        p = p_next;
+        valid = valid_next;
+        c = c_next;
+        nch = nch_next;
+    }
+}
+
+// A chunk as the MMA warp needs it, with its molecule's fields copied to registers.
+struct MmaItem {
+    const uint4* bpack;
+    int npad, nmchunk, npass, nch;
+    uint32_t ord;  // tile ordinal of the CTA
+    int pass, c;
+    unsigned km;   // kept columns of the chunk
+};
+
+// MMA warp: the next kept chunk after `it` inside its tile, in (pass, chunk) order.
+__device__ __forceinline__ bool mma_next_in_tile(const CtaState& S, MmaItem& it)
+{
+    const unsigned* km = S.kmask + (it.ord & 1) * MAX_CHUNKS;
+    for (;;) {
+        ++it.c;
+        if (it.c == it.nmchunk) {
+            it.c = -1;
+            if (++it.pass == it.npass) return false;
+            continue;
+        }
+        const unsigned k = km[it.c];
+        if (k != 0u) {
+            it.km = k;
+            return true;
+        }
+    }
+}
+
+// MMA warp: release the buffer of tile it.ord (unless it.ord is the first to
+// open), then open the following tiles (after the generation threads screened
+// them) until one has a kept chunk.  False when there are no more tiles.
+template <bool BATCH>
+__device__ __forceinline__ bool mma_open_next(const CtaState& S, MmaItem& it, bool release, int* status)
+{
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        if (release) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(S.bar_kfree + 8 * (it.ord & 1));
+            ++it.ord;
+        }
+        release = true;
+        const int b = it.ord & 1;
+        if (!mbar_wait(S.bar_screened + 8 * b, (it.ord >> 1) & 1u, status)) *S.abort_flag = 1;
+        if (S.tile_slot[b] < 0 || *S.abort_flag) return false;
+        const MolDesc& D = S.mol[BATCH ? b : 0];
+        it.bpack = D.bpack;
+        it.npad = D.npad;
+        it.nmchunk = D.B.nmchunk;
+        it.npass = D.npass;
+        it.nch = D.want_grad ? 4 : 1;
+        it.pass = 0;
+        it.c = -1;
+        if (mma_next_in_tile(S, it)) return true;
+    }
+}
+
+// MMA warp, lane 0: the bulk copy of an item's B block into stage seq % 2 once
+// that stage's previous MMAs are complete.
+__device__ __forceinline__ void mma_prefetch_b(const CtaState& S, const MmaItem& it, uint32_t seq, int* status)
+{
+    const uint32_t s = seq & 1u, u = seq >> 1;
+    const int bunits = 3 * it.npad * RUNITS;
+    if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
+    bulk_load(smem_u32(S.B_s + s * B_STAGE), it.bpack + ((long long)it.pass * it.nmchunk + it.c) * bunits,
+              (uint32_t)bunits * 16u, S.bar_bload + 8 * s);
+}
+
+// MMA side of the CTA (the last warp): for every kept chunk in order, the column
+// mask applied to its B block, then 48 MMAs (12 without gradient) from lane 0
+// once the generation threads filled the stage; the next chunk's B block is
+// requested halfway through, when the stage it goes to has been consumed.
+template <bool BATCH>
+__device__ __forceinline__ void mma_role(const CtaState& S, int* status)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t seq = 0, accseq = 0;
+    MmaItem cur;
+    cur.ord = 0;
+    bool have = mma_open_next<BATCH>(S, cur, false, status);
+    if (have && lane == 0) mma_prefetch_b(S, cur, seq, status);
+    int kq = 0;  // K-steps issued in the current job
+    while (have) {
+        const uint32_t s = seq & 1u, u = seq >> 1;
+        unsigned char* B_s = S.B_s + s * B_STAGE;
+        const int npad = cur.npad;
+        const int bunits = 3 * npad * RUNITS;
+        if (!mbar_wait(S.bar_bload + 8 * s, u & 1u, status)) *S.abort_flag = 1;
+        // columns of screened shells are zeroed.  Lane l touches the 16-byte units
+        // l, l + 32, ...: rows n = l / 4 (mod 8) of every part, physical unit l % 4, so
+        // with rows of 4 units and the 64-byte swizzle (unit ^ (n >> 1) % 4) always the
+        // same logical 8-column group
+        const unsigned m8 = (cur.km >> (8 * ((lane & 3) ^ ((lane >> 3) & 3)))) & 0xFFu;
+        if (m8 != 0xFFu) {
+            unsigned keep[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                keep[t] = ((m8 >> (2 * t)) & 1u ? 0x0000FFFFu : 0u) | ((m8 >> (2 * t + 1)) & 1u ? 0xFFFF0000u : 0u);
+            // bunits is a multiple of 192: six units per lane at a time, loads first
+            uint4* bu = (uint4*)B_s + lane;
+            for (int i = 0; i < bunits; i += 192) {
+                uint4 v[6];
+#pragma unroll
+                for (int j = 0; j < 6; ++j) v[j] = bu[i + 32 * j];
+#pragma unroll
+                for (int j = 0; j < 6; ++j)
+                    bu[i + 32 * j] = make_uint4(v[j].x & keep[0], v[j].y & keep[1], v[j].z & keep[2], v[j].w & keep[3]);
+            }
+            fence_proxy_async();
+        }
+        MmaItem nxt = cur;
+        const bool in_tile = mma_next_in_tile(S, nxt);  // the next chunk if it is in this tile
+        __syncwarp();
+        if (lane == 0) {
+            // the previous job's accumulators must have been read before they are overwritten
+            if (kq == 0 && accseq > 0 && !mbar_wait(S.bar_acc_empty, (accseq - 1) & 1u, status)) *S.abort_flag = 1;
+            if (!mbar_wait(S.bar_full + 8 * s, u & 1u, status)) *S.abort_flag = 1;
+            tc_fence_after();
+            const int nch = cur.nch;
+            const int pf = nch > 2 ? 1 : nch - 1;  // channel after which the next B block is requested
+            if (!*S.abort_flag) {
+                const uint32_t idesc = idesc_bf16(M, npad);
+                const uint32_t bpart16 = (uint32_t)(npad * ROWB) >> 4;
+                // descriptors differ only in the start-address field (bytes >> 4)
+                const uint64_t adesc = sdesc(smem_u32(S.A_s + s * A_STAGE)), bdesc = sdesc(smem_u32(B_s));
+#pragma unroll 1
+                for (int ch = 0; ch < nch; ++ch) {
+#pragma unroll
+                    for (int k = 0; k < KC / 16; ++k) {
+                        const int ks = kq + k;
+                        // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
+                        const int pa[6] = {0, 0, 1, 0, 1, 2};
+                        const int pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+                        for (int t = 0; t < 6; ++t) {
+                            const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 32) >> 4);
+                            const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
+                            uint32_t col, accf;
+                            if (ch == 0 && t == 0) {  // leading product -> accumulator ks mod 4
+                                col = ks & 3;
+                                accf = ks >= 4;
+                            } else if (ch == 0) {     // value corrections -> accumulator 4
+                                col = 4;
+                                accf = ks > 0 || t > 1;
+                            } else {                  // gradient channel ch -> accumulator 4 + ch
+                                col = 4 + ch;
+                                accf = ks > 0 || t > 0;
+                            }
+                            mma_bf16(S.tmem + col * npad, ad, bd, idesc, accf);
+                        }
+                    }
+                    if (ch == pf && in_tile) mma_prefetch_b(S, nxt, seq + 1, status);
+                }
+                mma_commit(S.bar_empty + 8 * s);
+            } else {
+                mbar_arrive(S.bar_empty + 8 * s);
+                if (in_tile) mma_prefetch_b(S, nxt, seq + 1, status);
+            }
+            if (!in_tile || nxt.pass != cur.pass) {
+                // last chunk of the job: hand the accumulators to the epilogue
+                if (!*S.abort_flag)
+                    mma_commit(S.bar_acc_full);
+                else
+                    mbar_arrive(S.bar_acc_full);
+            }
+        }
+        __syncwarp();
+        ++seq;
+        kq += KC / 16;
+        if (!in_tile || nxt.pass != cur.pass) {
+            ++accseq;
+            kq = 0;
+        }
+        have = in_tile;
+        if (!in_tile) {
+            // leave the tile once its last chunk's MMAs are issued; the next tile's
+            // first B block is requested as soon as the tile is open
+            have = mma_open_next<BATCH>(S, nxt, true, status);
+            if (have && lane == 0) mma_prefetch_b(S, nxt, seq, status);
+        }
+        cur = nxt;
+    }
 }
 
 // CTA set-up shared by the kernels: shared-memory carve-up, A stages zeroed
 // (columns of screened shells keep stale but finite values, multiplied by zeroed B
 // columns), mbarriers, TMEM allocation.  NTT threads in all, NTG of them generate.
 template <int NTT, int NTG>
-__device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_cols)
+__device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol, uint32_t tm_cols)
 {
     const int tid = threadIdx.x, warp = tid >> 5;
     CtaState S;
     S.A_s = smem;
     S.B_s = smem + NSTAGE * A_STAGE;
     S.kmask = (unsigned*)(S.B_s + NSTAGE * B_STAGE);
-    uint64_t* bar = (uint64_t*)(S.kmask + MAX_CHUNKS);  // full[2], empty[2], acc full, acc empty, bload[2]
-    uint32_t* tmem_slot = (uint32_t*)(bar + 8);
+    // full[2], empty[2], bload[2], acc full, acc empty, screened[2], kfree[2]
+    uint64_t* bar = (uint64_t*)(S.kmask + 2 * MAX_CHUNKS);
+    S.tile_slot = (long long*)(bar + 12);
+    uint32_t* tmem_slot = (uint32_t*)(S.tile_slot + 2);
     S.abort_flag = (int*)(tmem_slot + 1);
     S.bbox = (float*)(S.abort_flag + 1);
     S.bbox_part = S.bbox + 6;
     S.nkeep = (unsigned char*)(S.bbox_part + 24);
+    S.mol = mol;
     S.bar_full = smem_u32(bar);
     S.bar_empty = smem_u32(bar + 2);
-    S.bar_acc_full = smem_u32(bar + 4);
-    S.bar_acc_empty = smem_u32(bar + 5);
-    S.bar_bload = smem_u32(bar + 6);
+    S.bar_bload = smem_u32(bar + 4);
+    S.bar_acc_full = smem_u32(bar + 6);
+    S.bar_acc_empty = smem_u32(bar + 7);
+    S.bar_screened = smem_u32(bar + 8);
+    S.bar_kfree = smem_u32(bar + 10);
     for (int i = tid; i < NSTAGE * A_STAGE / 16; i += NTT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
@@ -717,6 +931,10 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
         }
         mbar_init(S.bar_acc_full, 1);
         mbar_init(S.bar_acc_empty, NTG);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(S.bar_screened + 8 * b, NTG);
+            mbar_init(S.bar_kfree + 8 * b, 1);
+        }
         *S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -734,10 +952,11 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, uint32_t tm_c
 }
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
-constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * MAX_CHUNKS + 8 * 8 + 4 + 4 + 4 * 6 + 4 * 24 +
-                              MAX_SHELLS + 64;
-static_assert(SMEM_BYTES <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
+constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * 2 * MAX_CHUNKS + 12 * 8 + 2 * 8 + 4 + 4 +
+                              4 * 6 + 4 * 24 + MAX_SHELLS + 64;
+static_assert(SMEM_BYTES + 2 * sizeof(MolDesc) <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 static_assert(KC == 32, "column masks are 32-bit and operand rows one 64-byte swizzle row");
+static_assert(sizeof(MolDesc) % 16 == 0, "descriptors are copied in 16-byte units");
 
 __device__ __forceinline__ void cta_teardown(const CtaState& S, uint32_t tm_cols)
 {
@@ -769,49 +988,55 @@ inline void tiling(const Grid& g, MolDesc& D)
     }
 }
 
+// Descriptor of one molecule's call (host side).
+inline void make_desc(MolDesc& D, const BasisDev& B, const Grid& g, const void* bpack, const double* occ, int npass,
+                      int npad, int nmo, int want_grad, double* rho, double* grad, long long ld)
+{
+    memset(&D, 0, sizeof(D));
+    D.B = B;
+    D.g = g;
+    D.bpack = (const uint4*)bpack;
+    D.occ = occ;
+    D.occf = (const float2*)(occ + 2 * npass * npad);
+    D.rho = rho;
+    D.grad = want_grad ? grad : nullptr;
+    D.ld = ld;
+    D.tile0 = 0;
+    D.npass = npass;
+    D.npad = npad;
+    D.nmo = nmo;
+    D.want_grad = want_grad;
+    tiling(g, D);
+}
+
 extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
 
+// Single molecule: its descriptor is copied to shared memory once.
 template <int NG>
-__global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_kernel(const Params P)
+__global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_kernel(const __grid_constant__ Params P)
 {
+    __shared__ MolDesc mol[1];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    const uint32_t tm_cols = tmem_cols_for(P.npad);
-    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, tm_cols);
-    MolDesc D;
-    D.B = P.B;
-    D.g = P.g;
-    D.bpack = P.bpack;
-    D.occ = P.occ;
-    D.occf = (const float2*)(P.occ + 2 * P.npass * P.npad);
-    D.rho = P.rho;
-    D.grad = P.grad;
-    D.ld = P.ld;
-    D.tile0 = 0;
-    D.npass = P.npass;
-    D.npad = P.npad;
-    D.nmo = P.nmo;
-    D.want_grad = P.want_grad;
-    D.brick = P.brick;
-    D.nby = P.nby;
-    D.nbz = P.nbz;
-    D.ntiles = P.ntiles;
-    Pipe pp;
-    __shared__ long long next_tile;
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) next_tile = (long long)atomicAdd(P.counter, 1ull);
-        __syncthreads();
-        const long long tile = next_tile;
-        if (tile >= P.ntiles || *S.abort_flag) break;
-        mixed_tile<NG>(D, tile, S, pp, P.status);
-    }
+    if (threadIdx.x < sizeof(MolDesc) / 16) ((uint4*)mol)[threadIdx.x] = ((const uint4*)&P.D)[threadIdx.x];
+    const uint32_t tm_cols = tmem_cols_for(P.D.npad);
+    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, mol, tm_cols);
+    TileFeed F;
+    F.counter = P.counter;
+    F.ntiles = P.D.ntiles;
+    F.descs = nullptr;
+    F.nmol = 1;
+    F.grab = 1;
+    if (threadIdx.x < 128 * NG)
+        gen_role<NG, false>(F, S, P.status);
+    else
+        mma_role<false>(S, P.status);
     cta_teardown(S, tm_cols);
 }
 
-// Batched launch: one persistent CTA per SM takes `grab` consecutive tiles of
-// the concatenated tile numbering at a time from a global counter (zeroed before
-// the launch), finds the molecule by binary search over tile0 and copies its
-// descriptor to shared memory when the molecule changes.
+// Batched launch: one persistent CTA per SM; warp 0 takes `grab` consecutive
+// tiles of the concatenated tile numbering at a time from a global counter
+// (zeroed before the launch), finds each tile's molecule by binary search over
+// tile0 and copies its descriptor into the tile's buffer.
 struct BatchParams {
     const MolDesc* descs;  // nmol, ascending tile0
     int nmol;
@@ -824,46 +1049,29 @@ struct BatchParams {
 template <int NG>
 __global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_batch_kernel(const BatchParams P)
 {
+    __shared__ MolDesc mol[2];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, 512);
-    __shared__ MolDesc Dsh;
-    __shared__ long long work;
-    __shared__ int cur_mol;
-    if (threadIdx.x == 0) cur_mol = -1;
-    Pipe pp;
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) work = (long long)atomicAdd(P.counter, (unsigned long long)P.grab);
-        __syncthreads();
-        const long long t0 = work;
-        if (t0 >= P.total_tiles || *S.abort_flag) break;
-        const long long t1 = t0 + P.grab < P.total_tiles ? t0 + P.grab : P.total_tiles;
-        for (long long t = t0; t < t1; ++t) {
-            __syncthreads();  // every thread is done with the previous tile's descriptor
-            if (threadIdx.x == 0) {
-                int lo = 0, hi = P.nmol - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (P.descs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
-                }
-                if (lo != cur_mol) {
-                    Dsh = P.descs[lo];
-                    cur_mol = lo;
-                }
-            }
-            __syncthreads();
-            if (*S.abort_flag) break;  // read between two barriers: the same value in every thread
-            mixed_tile<NG>(Dsh, t - Dsh.tile0, S, pp, P.status);
-        }
-    }
+    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, mol, 512);
+    TileFeed F;
+    F.counter = P.counter;
+    F.ntiles = P.total_tiles;
+    F.descs = P.descs;
+    F.nmol = P.nmol;
+    F.grab = P.grab;
+    if (threadIdx.x < 128 * NG)
+        gen_role<NG, true>(F, S, P.status);
+    else
+        mma_role<true>(S, P.status);
     cta_teardown(S, 512);
 }
 
-// Split C_eff (nmo x ncart, FP64) into three BF16 parts in the B operand layout:
+// Split C_eff (nmo x ncart, FP64) times the columns' angular norms into three
+// BF16 parts in the B operand layout:
 // bpack[pass][chunk][part] is an npad x 32 K-major SWIZZLE_64B tile whose column
 // kk holds the coefficient of the listed Cartesian AO feeding mixed column kk.
 __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, const int* __restrict__ mcol_cart,
-                              int nmchunk, int npass, int npad, __nv_bfloat16* __restrict__ bpack)
+                              const double* __restrict__ mcol_g, int nmchunk, int npass, int npad,
+                              __nv_bfloat16* __restrict__ bpack)
 {
     const long long total = (long long)npass * nmchunk * npad * KC;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
@@ -874,7 +1082,7 @@ __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, 
         const int pass = (int)(i / ((long long)KC * npad * nmchunk));
         const int mo = pass * npad + n;
         const int cart = mcol_cart[c * KC + kk];
-        double v = (mo < nmo && cart >= 0) ? C[(long long)mo * ncart + cart] : 0.0;
+        double v = (mo < nmo && cart >= 0) ? C[(long long)mo * ncart + cart] * mcol_g[c * KC + kk] : 0.0;
         const __nv_bfloat16 h0 = __double2bfloat16(v);
         const double r1 = v - (double)__bfloat162float(h0);
         const __nv_bfloat16 h1 = __double2bfloat16(r1);
@@ -1037,7 +1245,7 @@ extern "C" int okg_mixed_set_coeffs(okg_mixed_plan* p, const double* d_coeff, co
     if (!p || !d_coeff || !d_occ) return set_error(OKG_ERR_ARG, "okg_mixed_set_coeffs: NULL argument");
     cudaStream_t st = (cudaStream_t)stream;
     const BasisDev& B = p->basis->dev;
-    mx::pack_b_kernel<<<p->sm_count * 4, 256, 0, st>>>(d_coeff, p->nmo, B.ncart, B.mcol_cart, B.nmchunk, p->npass,
+    mx::pack_b_kernel<<<p->sm_count * 4, 256, 0, st>>>(d_coeff, p->nmo, B.ncart, B.mcol_cart, B.mcol_g, B.nmchunk, p->npass,
                                                        p->npad, p->bpack);
     const int total = p->npass * p->npad;
     mx::pack_occ_kernel<<<(total + 127) / 128, 128, 0, st>>>(d_occ, p->nmo, total, p->occ);
@@ -1065,30 +1273,14 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     if (g.npts == 0) return OKG_OK;
     if (ld < g.npts) return set_error(OKG_ERR_ARG, "okg_rho_mixed: ld < npts");
     mx::Params P;
-    P.B = p->basis->dev;
-    P.g = g;
-    P.bpack = (const uint4*)p->bpack;
-    P.occ = p->occ;
-    P.npass = p->npass;
-    P.npad = p->npad;
-    P.nmo = p->nmo;
-    P.want_grad = want_grad;
-    P.rho = d_rho;
-    P.grad = d_grad;
-    P.ld = ld;
+    mx::make_desc(P.D, p->basis->dev, g, p->bpack, p->occ, p->npass, p->npad, p->nmo, want_grad, d_rho, d_grad, ld);
     P.status = p->status;
     P.counter = (unsigned long long*)((char*)p->status + 64);
     {
         cudaError_t e0 = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), (cudaStream_t)stream);
         if (e0 != cudaSuccess) return cuda_status(e0, "okg_rho_mixed: counter reset");
     }
-    mx::MolDesc T;
-    mx::tiling(g, T);
-    P.ntiles = T.ntiles;
-    P.brick = T.brick;
-    P.nby = T.nby;
-    P.nbz = T.nbz;
-    const long long grid = P.ntiles < p->sm_count ? P.ntiles : p->sm_count;
+    const long long grid = P.D.ntiles < p->sm_count ? P.D.ntiles : p->sm_count;
     mx::launch_single(p->ngen, (unsigned)grid, (cudaStream_t)stream, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
 }
@@ -1126,28 +1318,19 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
             return set_error(OKG_ERR_ARG, "okg_batch_create: regular grid range outside Nx*Ny*Nz");
         if (ld[m] < gr->npts) return set_error(OKG_ERR_ARG, "okg_batch_create: ld < npts");
         mx::MolDesc& D = descs[m];
-        D.B = p->basis->dev;
-        D.g.x = gr->d_x;
-        D.g.y = gr->d_y;
-        D.g.z = gr->d_z;
-        D.g.npts = gr->npts;
-        D.g.offset = gr->offset;
-        D.g.nx = gr->nx;
-        D.g.ny = gr->ny;
-        D.g.nz = gr->nz;
-        D.g.regular = gr->regular;
-        D.bpack = (const uint4*)p->bpack;
-        D.occ = p->occ;
-        D.occf = (const float2*)(p->occ + 2 * p->npass * p->npad);
-        D.rho = d_rho[m];
-        D.grad = want_grad ? d_grad[m] : nullptr;
-        D.ld = ld[m];
-        mx::tiling(D.g, D);
+        Grid g;
+        g.x = gr->d_x;
+        g.y = gr->d_y;
+        g.z = gr->d_z;
+        g.npts = gr->npts;
+        g.offset = gr->offset;
+        g.nx = gr->nx;
+        g.ny = gr->ny;
+        g.nz = gr->nz;
+        g.regular = gr->regular;
+        mx::make_desc(D, p->basis->dev, g, p->bpack, p->occ, p->npass, p->npad, p->nmo, want_grad, d_rho[m],
+                      want_grad ? d_grad[m] : nullptr, ld[m]);
         D.tile0 = tile0;
-        D.npass = p->npass;
-        D.npad = p->npad;
-        D.nmo = p->nmo;
-        D.want_grad = want_grad;
         tile0 += D.ntiles;
         sms = p->sm_count;
     }
@@ -1366,31 +1549,16 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     e = cudaMemsetAsync(status, 0, sizeof(int), st);
     if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: clear status");
     const BasisDev& B = b->dev;
-    pack_b_kernel<<<nd->sm_count * 4, 256, 0, st>>>(d_coeff, nmo, B.ncart, B.mcol_cart, B.nmchunk, npass, npad, bpack);
+    pack_b_kernel<<<nd->sm_count * 4, 256, 0, st>>>(d_coeff, nmo, B.ncart, B.mcol_cart, B.mcol_g, B.nmchunk, npass, npad,
+                                                    bpack);
     pack_occ_kernel<<<(npass * npad + 127) / 128, 128, 0, st>>>(d_occ, nmo, npass * npad, occ);
     Params P;
-    P.B = B;
-    P.g = g;
-    P.bpack = (const uint4*)bpack;
-    P.occ = occ;
-    P.npass = npass;
-    P.npad = npad;
-    P.nmo = nmo;
-    P.want_grad = want_grad;
-    P.rho = d_rho;
-    P.grad = d_grad;
-    P.ld = ld;
+    make_desc(P.D, B, g, bpack, occ, npass, npad, nmo, want_grad, d_rho, d_grad, ld);
     P.status = status;
     P.counter = (unsigned long long*)(nd->base + st_off + 64);
     e = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: counter reset");
-    MolDesc T;
-    tiling(g, T);
-    P.ntiles = T.ntiles;
-    P.brick = T.brick;
-    P.nby = T.nby;
-    P.nbz = T.nbz;
-    const long long grid = P.ntiles < nd->sm_count ? P.ntiles : nd->sm_count;
+    const long long grid = P.D.ntiles < nd->sm_count ? P.D.ntiles : nd->sm_count;
     launch_single(NG_DEFAULT, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed_noalloc launch");
 }
