@@ -135,9 +135,14 @@ int okg_mixed_plan_create(const okg_basis* basis, int nmo, okg_mixed_plan** out)
  * autotuner -- fewer columns per pass, more passes. */
 int okg_mixed_plan_create_tiled(const okg_basis* basis, int nmo, int n_max, okg_mixed_plan** out);
 int okg_mixed_plan_destroy(okg_mixed_plan* plan);
-/* Threads per CTA of the plan's launches: 256, 384 or 512 (2, 3 or 4 threads share the
- * AO generation of each of the tile's 128 points). */
+/* AO-generation threads per CTA of the plan's launches: 256, 384 or 512, one grid
+ * point each (2, 3 or 4 threads share the AO generation of each of the tile's 128
+ * points); one more warp issues the tensor-core work. */
 int okg_mixed_plan_set_threads(okg_mixed_plan* plan, int threads);
+/* The same with the grid points per generation thread: (256, 1), (384, 1), (512, 1),
+ * (256, 2) or (384, 2).  With 2 points a thread generates two adjacent points of the
+ * tile (packed conversions and stores); default (384, 1). */
+int okg_mixed_plan_set_generation(okg_mixed_plan* plan, int threads, int points_per_thread);
 /* Split C_eff (nmo x ncart, FP64, device) into the BF16 operand tiles; copy occ (nmo). */
 int okg_mixed_set_coeffs(okg_mixed_plan* plan, const double* d_coeff, const double* d_occ, okg_stream stream);
 /* d_rho[i]; d_grad[c * ld + i] for c = x, y, z when want_grad. */
@@ -162,6 +167,9 @@ int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* gri
                      double* const* d_grad, const int64_t* ld, int want_grad, okg_batch** out);
 int okg_batch_destroy(okg_batch* batch);
 int okg_batch_set_schedule(okg_batch* batch, int tiles_per_grab, int ctas, int threads);
+/* Generation threads and grid points per generation thread as for
+ * okg_mixed_plan_set_generation (after okg_batch_set_schedule, which sets one point). */
+int okg_batch_set_generation(okg_batch* batch, int threads, int points_per_thread);
 int okg_batch_tiles(const okg_batch* batch, long long* total_tiles);
 int okg_batch_run(okg_batch* batch, okg_stream stream);
 int okg_batch_status(okg_batch* batch, int* device_status);

@@ -56,7 +56,6 @@ constexpr int M = 128;
 constexpr int KC = OKG_MKC;           // 32 BF16 = 64 bytes
 constexpr int ROWB = KC * 2;          // bytes of one operand row
 constexpr int RUNITS = ROWB / 16;     // 16-byte units of one operand row
-constexpr int NG_DEFAULT = 3;         // generation groups per point (generation threads = 128 x groups)
 constexpr int A_TILE = M * ROWB;      // bytes of one 128 x 32 BF16 sub-tile
 constexpr int A_STAGE = 12 * A_TILE;  // 4 channels x 3 parts
 constexpr int NMAX = 64;              // MO columns per pass
@@ -69,7 +68,8 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p)
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// SMEM matrix descriptor: K-major, SWIZZLE_64B, SBO = 512 B (8-row group stride).
+// SMEM matrix descriptor of the B operand: K-major, SWIZZLE_64B, SBO = 512 B
+// (8-row group stride).
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr)
 {
     uint64_t d = 0;
@@ -81,10 +81,26 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr)
     return d;
 }
 
-// Instruction descriptor: kind::f16, A = B = BF16, D = F32, K-major A and B.
+// SMEM matrix descriptor of the A operand: M-major (grid points contiguous),
+// SWIZZLE_128B: atoms of 64 points x 8 K (1024 B), the two 64-point halves of the
+// tile 1024 B apart (leading byte offset), 8-K groups 2048 B apart (stride byte
+// offset).
+__device__ __forceinline__ uint64_t adesc_mn(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)(1024 >> 4) << 16;       // leading byte offset: next 64 points
+    d |= (uint64_t)(2048 >> 4) << 32;       // stride byte offset: next 8 K
+    d |= (uint64_t)1 << 46;                 // descriptor version
+    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, M-major A, K-major B.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M_, int N_)
 {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N_ >> 3) << 17) | ((uint32_t)(M_ >> 4) << 24);
+    return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | ((uint32_t)(N_ >> 3) << 17) |
+           ((uint32_t)(M_ >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
@@ -215,11 +231,19 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16& b0, __nv_bfloat16
 }
 
 // byte offset of element (row m, column k) in a K-major BF16 tile with 32-element
-// rows and SWIZZLE_64B: 8-row groups of 512 B, the 16-byte unit index XORed with
-// address bits 7..8, i.e. (m >> 1) & 3
+// rows and SWIZZLE_64B (the B operand): 8-row groups of 512 B, the 16-byte unit
+// index XORed with address bits 7..8, i.e. (m >> 1) & 3
 __host__ __device__ __forceinline__ uint32_t sw64_off(int m, int k)
 {
     return (uint32_t)((m >> 3) * 512 + (m & 7) * 64 + ((((k >> 3) ^ (m >> 1)) & 3) << 4) + ((k & 7) << 1));
+}
+
+// byte offset of element (point m, column k) of the 128 x 32 M-major SWIZZLE_128B A
+// tile: 128-byte rows of 64 consecutive points for one column, the 16-byte unit
+// index XORed with the row's position in its 8-row atom (k % 8)
+__device__ __forceinline__ uint32_t amn_off(int m, int k)
+{
+    return (uint32_t)((m >> 6) * 1024 + (k >> 3) * 2048 + (k & 7) * 128 + ((((m >> 3) ^ k) & 7) << 4) + ((m & 7) << 1));
 }
 
 // One molecule as seen by a tile: its basis tables, grid, coefficient tiles and outputs.
@@ -390,12 +414,17 @@ struct TileFeed {
 // bounding box and the screening of every shell against it; then each thread
 // arrives on the buffer's "screened" barrier.  Returns the tile (local to its
 // molecule) or -1 when there are no more.
-template <int NG, bool BATCH>
+// Grid points of a generation thread: P consecutive rows of the tile.
+template <int P>
+struct GenPts {
+    double x[P], y[P], z[P];
+};
+
+template <int NTG, int P, bool BATCH>
 __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const CtaState& S, uint32_t ord,
                                                       long long& gnext, long long& gend, long long& p, bool& valid,
-                                                      double& x, double& y, double& z, int* status)
+                                                      GenPts<P>& gp, int* status)
 {
-    constexpr int NTG = 128 * NG;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int b = ord & 1;
     if (ord >= 2 && !mbar_wait(S.bar_kfree + 8 * b, ((ord >> 1) - 1) & 1u, status)) *S.abort_flag = 1;
@@ -446,18 +475,29 @@ __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const C
     }
     const MolDesc& D = S.mol[BATCH ? b : 0];
     const BasisDev& B = D.B;
-    valid = tile_point(D, tile, tid & (M - 1), p);
-    grid_point(D.g, p, x, y, z);
+    // the point this thread stores (TMEM lane 32 (warp % 4) + lane of the epilogue)
+    valid = tile_point(D, tile, 32 * (warp & 3) + lane, p);
+    // the points this thread generates: rows P (tid % (128 / P)) + i
+    float v[6] = {3.0e38f, 3.0e38f, 3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+        long long pg;
+        const bool vg = tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
+        grid_point(D.g, pg, gp.x[i], gp.y[i], gp.z[i]);
+        if (vg) {
+            const float fx = dbl_to_flt_rn(gp.x[i]), fy = dbl_to_flt_rn(gp.y[i]), fz = dbl_to_flt_rn(gp.z[i]);
+            v[0] = fminf(v[0], fx);
+            v[1] = fminf(v[1], fy);
+            v[2] = fminf(v[2], fz);
+            v[3] = fmaxf(v[3], fx);
+            v[4] = fmaxf(v[4], fy);
+            v[5] = fmaxf(v[5], fz);
+        }
+    }
     unsigned* km = S.kmask + b * MAX_CHUNKS;
-    // bounding box of the tile's valid points (rows 0..127 = warps 0..3)
-    if (warp < 4) {
-        float v[6];
-        v[0] = valid ? dbl_to_flt_rn(x) : 3.0e38f;
-        v[1] = valid ? dbl_to_flt_rn(y) : 3.0e38f;
-        v[2] = valid ? dbl_to_flt_rn(z) : 3.0e38f;
-        v[3] = valid ? dbl_to_flt_rn(x) : -3.0e38f;
-        v[4] = valid ? dbl_to_flt_rn(y) : -3.0e38f;
-        v[5] = valid ? dbl_to_flt_rn(z) : -3.0e38f;
+    // bounding box of the tile's valid points (generation group 0 = warps 0 .. 4 / P - 1)
+    constexpr int BW = 4 / P;
+    if (warp < BW) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -472,7 +512,7 @@ __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const C
     gen_sync<NTG>();
     if (tid < 6) {
         float a = S.bbox_part[tid];
-        for (int w = 1; w < 4; ++w)
+        for (int w = 1; w < BW; ++w)
             a = tid < 3 ? fminf(a, S.bbox_part[w * 6 + tid]) : fmaxf(a, S.bbox_part[w * 6 + tid]);
         S.bbox[tid] = a;
     }
@@ -498,22 +538,72 @@ __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const C
 
 // Atoms of a job go round-robin to the generation groups in the order of the
 // job's shells; the group owning an atom keeps its r^2 and coordinates.
-struct AtomRun {
+struct AtomRunBase {
     int last_atom = -1, ord = -1;
     bool mine = false;
-    double rr = 0;
-    float X = 0, Y = 0, Z = 0;
+};
+template <int P>
+struct AtomRun : AtomRunBase {
+    double rr[P];
+    float X[P], Y[P], Z[P];
 };
 
-// Generation threads: the AO values (4 or 1 channels x 3 BF16 parts) of one kept
-// chunk for this thread's point and atoms, into the next stage of the ring.
-template <int NG>
-__device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaState& S, uint32_t& seq, AtomRun& ar,
-                                          unsigned chmask, double x, double y, double z, int* status)
+// All canonical components of an L shell at two points, for the channels in
+// chmask: sink(channel, canonical index, value at point 0, value at point 1).
+template <int L, typename Sink2>
+__device__ __forceinline__ void shell_eval2(const float (&X)[2], const float (&Y)[2], const float (&Z)[2],
+                                            const Radial<float> (&r)[2], unsigned chmask, Sink2&& sink)
 {
+    float px[2][L + 3], py[2][L + 3], pz[2][L + 3];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        px[i][0] = py[i][0] = pz[i][0] = 1.f;
+#pragma unroll
+        for (int e = 1; e < L + 3; ++e) {
+            px[i][e] = px[i][e - 1] * X[i];
+            py[i][e] = py[i][e - 1] * Y[i];
+            pz[i][e] = pz[i][e - 1] * Z[i];
+        }
+    }
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+        if (!(chmask & (1u << ch))) continue;
+        [&]<int... J>(std::integer_sequence<int, J...>) {
+            (sink(ch, J,
+                  channel_poly<canon_l(L, J, 0), canon_l(L, J, 1), canon_l(L, J, 2), float>(ch, px[0], py[0], pz[0],
+                                                                                           r[0], false),
+                  channel_poly<canon_l(L, J, 0), canon_l(L, J, 1), canon_l(L, J, 2), float>(ch, px[1], py[1], pz[1],
+                                                                                           r[1], false)),
+             ...);
+        }(std::make_integer_sequence<int, ncanon(L)>{});
+    }
+}
+
+template <typename Sink2>
+__device__ __forceinline__ void shell_eval2_L(int L, const float (&X)[2], const float (&Y)[2], const float (&Z)[2],
+                                              const Radial<float> (&r)[2], unsigned chmask, Sink2&& sink)
+{
+    switch (L) {
+    case 0: shell_eval2<0>(X, Y, Z, r, chmask, sink); break;
+    case 1: shell_eval2<1>(X, Y, Z, r, chmask, sink); break;
+    case 2: shell_eval2<2>(X, Y, Z, r, chmask, sink); break;
+    case 3: shell_eval2<3>(X, Y, Z, r, chmask, sink); break;
+    default: shell_eval2<4>(X, Y, Z, r, chmask, sink); break;
+    }
+}
+
+// Generation threads: the AO values (4 or 1 channels x 3 BF16 parts) of one kept
+// chunk for this thread's P points and atoms, into the next stage of the ring.
+// With P = 2 the two points are adjacent in the M-major tile: each part of a
+// value pair is one packed conversion and one 4-byte store.
+template <int NTG, int P>
+__device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaState& S, uint32_t& seq, AtomRun<P>& ar,
+                                          unsigned chmask, const GenPts<P>& gp, int* status)
+{
+    constexpr int NG = NTG * P / 128;  // generation groups
     const int tid = threadIdx.x;
-    const int prow = tid & (M - 1);  // point row of this thread in the tile
-    const int grp = tid >> 7;        // generation group
+    const int r0 = P * (tid % (128 / P));  // first point row of this thread
+    const int grp = tid / (128 / P);
     const uint32_t s = seq & 1u, u = seq >> 1;
     unsigned char* A_s = S.A_s + s * A_STAGE;
     if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
@@ -527,41 +617,69 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaSta
             ++ar.ord;
             ar.mine = ar.ord % NG == grp;
             if (ar.mine) {
-                const double X = x - B.atoms[4 * sh.atom];
-                const double Y = y - B.atoms[4 * sh.atom + 1];
-                const double Z = z - B.atoms[4 * sh.atom + 2];
-                ar.rr = X * X + Y * Y + Z * Z;
-                ar.X = dbl_to_flt_rn(X);
-                ar.Y = dbl_to_flt_rn(Y);
-                ar.Z = dbl_to_flt_rn(Z);
+                const double ax = B.atoms[4 * sh.atom], ay = B.atoms[4 * sh.atom + 1], az = B.atoms[4 * sh.atom + 2];
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    const double X = gp.x[i] - ax, Y = gp.y[i] - ay, Z = gp.z[i] - az;
+                    ar.rr[i] = X * X + Y * Y + Z * Z;
+                    ar.X[i] = dbl_to_flt_rn(X);
+                    ar.Y[i] = dbl_to_flt_rn(Y);
+                    ar.Z[i] = dbl_to_flt_rn(Z);
+                }
             }
         }
         if (!ar.mine) continue;
         const int nk = S.nkeep[si];
         if (nk == 0) continue;
-        // primitives two at a time (two independent exponentials in flight)
-        float R0 = 0.f, R1 = 0.f;
-        for (int k = 0; k < nk; k += 2) {
-            const PrimMx pa = B.prim_mx[sh.prim0 + k];
-            const float ea = exp2_neg(pa.a2 * ar.rr);
-            if (k + 1 < nk) {
-                const PrimMx pb = B.prim_mx[sh.prim0 + k + 1];
-                const float eb = exp2_neg(pb.a2 * ar.rr);
-                R0 = fmaf(pb.w, eb, R0);
-                R1 = fmaf(pb.wa, eb, R1);
+        if constexpr (P == 1) {
+            // primitives two at a time (two independent exponentials in flight)
+            float R0 = 0.f, R1 = 0.f;
+            for (int k = 0; k < nk; k += 2) {
+                const PrimMx pa = B.prim_mx[sh.prim0 + k];
+                const float ea = exp2_neg(pa.a2 * ar.rr[0]);
+                if (k + 1 < nk) {
+                    const PrimMx pb = B.prim_mx[sh.prim0 + k + 1];
+                    const float eb = exp2_neg(pb.a2 * ar.rr[0]);
+                    R0 = fmaf(pb.w, eb, R0);
+                    R1 = fmaf(pb.wa, eb, R1);
+                }
+                R0 = fmaf(pa.w, ea, R0);
+                R1 = fmaf(pa.wa, ea, R1);
             }
-            R0 = fmaf(pa.w, ea, R0);
-            R1 = fmaf(pa.wa, ea, R1);
+            const Radial<float> r{R0, R1, 0.f};
+            shell_eval_L(sh.L, ar.X[0], ar.Y[0], ar.Z[0], r, chmask, false, [&](int ch, int j, float v) {
+                __nv_bfloat16 b0, b1, b2;
+                split3(v, b0, b1, b2);
+                unsigned char* base = A_s + ch * 3 * A_TILE + amn_off(r0, sh.mcol + j);
+                *(__nv_bfloat16*)(base) = b0;
+                *(__nv_bfloat16*)(base + A_TILE) = b1;
+                *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
+            });
+        } else {
+            Radial<float> r[2] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            for (int k = 0; k < nk; ++k) {
+                const PrimMx pm = B.prim_mx[sh.prim0 + k];
+                const float e0 = exp2_neg(pm.a2 * ar.rr[0]);
+                const float e1 = exp2_neg(pm.a2 * ar.rr[1]);
+                r[0].R0 = fmaf(pm.w, e0, r[0].R0);
+                r[0].R1 = fmaf(pm.wa, e0, r[0].R1);
+                r[1].R0 = fmaf(pm.w, e1, r[1].R0);
+                r[1].R1 = fmaf(pm.wa, e1, r[1].R1);
+            }
+            shell_eval2_L(sh.L, ar.X, ar.Y, ar.Z, r, chmask, [&](int ch, int j, float v0, float v1) {
+                // v = b0 + b1 + b2 to 2^-24 for both points, each part a packed pair
+                const __nv_bfloat162 h0 = __floats2bfloat162_rn(v0, v1);
+                const float2 f0 = __bfloat1622float2(h0);
+                const float s0 = v0 - f0.x, s1 = v1 - f0.y;
+                const __nv_bfloat162 h1 = __floats2bfloat162_rn(s0, s1);
+                const float2 f1 = __bfloat1622float2(h1);
+                const __nv_bfloat162 h2 = __floats2bfloat162_rn(s0 - f1.x, s1 - f1.y);
+                unsigned char* base = A_s + ch * 3 * A_TILE + amn_off(r0, sh.mcol + j);
+                *(__nv_bfloat162*)(base) = h0;
+                *(__nv_bfloat162*)(base + A_TILE) = h1;
+                *(__nv_bfloat162*)(base + 2 * A_TILE) = h2;
+            });
         }
-        const Radial<float> r{R0, R1, 0.f};
-        shell_eval_L(sh.L, ar.X, ar.Y, ar.Z, r, chmask, false, [&](int ch, int j, float v) {
-            __nv_bfloat16 b0, b1, b2;
-            split3(v, b0, b1, b2);
-            unsigned char* base = A_s + ch * 3 * A_TILE + sw64_off(prow, sh.mcol + j);
-            *(__nv_bfloat16*)(base) = b0;
-            *(__nv_bfloat16*)(base + A_TILE) = b1;
-            *(__nv_bfloat16*)(base + 2 * A_TILE) = b2;
-        });
     }
     fence_proxy_async();
     mbar_arrive(S.bar_full + 8 * s);
@@ -570,10 +688,10 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaSta
 
 // Generation threads: the epilogue of one job.  Warp w reads TMEM lanes
 // 32 (w % 4) .. (its 32 points) and owns the outputs o (0 = rho, 1..3 = d/dx,
-// d/dy, d/dz) with o % NG == w / 4; the 8-MO groups are reduced in double-float
+// d/dy, d/dz) with o % E == w / 4 (E = generation warps / 4); the 8-MO groups are reduced in double-float
 // FP32 (exact products by FMA, two-sum accumulation, about 44 bits) and added to
 // the FP64 accumulators.
-template <int NG>
+template <int E>
 __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nchunks, const CtaState& S,
                                              uint32_t& accseq, double (&acc)[4], int* status)
 {
@@ -582,7 +700,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nch
     const int npad = D.npad;
     bool own[4];
 #pragma unroll
-    for (int o = 0; o < 4; ++o) own[o] = (o % NG == h) && (o == 0 || D.want_grad);
+    for (int o = 0; o < 4; ++o) own[o] = (o % E == h) && (o == 0 || D.want_grad);
     if (!mbar_wait(S.bar_acc_full, accseq & 1u, status)) *S.abort_flag = 1;
     ++accseq;
     tc_fence_after();
@@ -637,19 +755,20 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nch
 // first chunk of the next job (screening its tile first when it starts one) is
 // generated before the epilogue of the current job, so the tensor core's tail
 // of a job overlaps useful work.
-template <int NG, bool BATCH>
+template <int NTG, int P, bool BATCH>
 __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, int* status)
 {
+    constexpr int E = NTG / 128;  // epilogue warps per TMEM lane quarter
     const int warp = threadIdx.x >> 5;
     const int h = warp >> 2;
     uint32_t seq = 0, accseq = 0, ord = 0;
     long long gnext = 0, gend = 0;
     long long p = 0;
     bool valid = false;
-    double x = 0, y = 0, z = 0;
-    if (fetch_and_screen<NG, BATCH>(F, S, ord, gnext, gend, p, valid, x, y, z, status) < 0) return;
+    GenPts<P> gp;
+    if (fetch_and_screen<NTG, P, BATCH>(F, S, ord, gnext, gend, p, valid, gp, status) < 0) return;
     int gpass = 0;
-    AtomRun ar;
+    AtomRun<P> ar;
     int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
     int nch = 0;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -660,7 +779,7 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
             const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
             const BasisDev& B = Dg.B;
             while (c >= 0) {
-                gen_chunk<NG>(B, c, S, seq, ar, chmask, x, y, z, status);
+                gen_chunk<NTG, P>(B, c, S, seq, ar, chmask, gp, status);
                 ++nch;
                 c = next_kept(km, B.nmchunk, c);
             }
@@ -673,29 +792,29 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
         if (npass_next == Dg.npass) {
             ord_next = ord + 1;
             npass_next = 0;
-            more = fetch_and_screen<NG, BATCH>(F, S, ord_next, gnext, gend, p_next, valid_next, x, y, z, status) >= 0;
+            more = fetch_and_screen<NTG, P, BATCH>(F, S, ord_next, gnext, gend, p_next, valid_next, gp, status) >= 0;
         }
         int c_next = -1, nch_next = 0;
         if (more) {
             const MolDesc& Dn = S.mol[BATCH ? (ord_next & 1) : 0];
             const unsigned* kmn = S.kmask + (ord_next & 1) * MAX_CHUNKS;
-            ar = AtomRun();
+            ar = AtomRun<P>();
             c_next = next_kept(kmn, Dn.B.nmchunk, -1);
             if (c_next >= 0) {
-                gen_chunk<NG>(Dn.B, c_next, S, seq, ar, Dn.want_grad ? 0xFu : 0x1u, x, y, z, status);
+                gen_chunk<NTG, P>(Dn.B, c_next, S, seq, ar, Dn.want_grad ? 0xFu : 0x1u, gp, status);
                 ++nch_next;
                 c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
             }
         }
         // the current job's epilogue (nothing to read if none of its chunks reached the tile)
-        if (nch > 0) gen_epilogue<NG>(Dg, gpass, nch, S, accseq, acc, status);
+        if (nch > 0) gen_epilogue<E>(Dg, gpass, nch, S, accseq, acc, status);
         if (gpass == Dg.npass - 1) {
             if (valid && !*S.abort_flag) {
-                if (0 % NG == h) Dg.rho[p] = acc[0];
+                if (0 % E == h) Dg.rho[p] = acc[0];
                 if (Dg.want_grad) {
 #pragma unroll
                     for (int o = 1; o < 4; ++o)
-                        if (o % NG == h) Dg.grad[(long long)(o - 1) * Dg.ld + p] = acc[o];
+                        if (o % E == h) Dg.grad[(long long)(o - 1) * Dg.ld + p] = acc[o];
                 }
             }
 #pragma unroll
@@ -835,7 +954,7 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
                 const uint32_t idesc = idesc_bf16(M, npad);
                 const uint32_t bpart16 = (uint32_t)(npad * ROWB) >> 4;
                 // descriptors differ only in the start-address field (bytes >> 4)
-                const uint64_t adesc = sdesc(smem_u32(S.A_s + s * A_STAGE)), bdesc = sdesc(smem_u32(B_s));
+                const uint64_t adesc = adesc_mn(smem_u32(S.A_s + s * A_STAGE)), bdesc = sdesc(smem_u32(B_s));
 #pragma unroll 1
                 for (int ch = 0; ch < nch; ++ch) {
 #pragma unroll
@@ -846,7 +965,7 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
                         const int pb[6] = {0, 1, 0, 2, 1, 0};
 #pragma unroll
                         for (int t = 0; t < 6; ++t) {
-                            const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 32) >> 4);
+                            const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 4096) >> 4);
                             const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
                             uint32_t col, accf;
                             if (ch == 0 && t == 0) {  // leading product -> accumulator ks mod 4
@@ -1012,22 +1131,22 @@ inline void make_desc(MolDesc& D, const BasisDev& B, const Grid& g, const void* 
 extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
 
 // Single molecule: its descriptor is copied to shared memory once.
-template <int NG>
-__global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_kernel(const __grid_constant__ Params P)
+template <int NTG, int PP>
+__global__ void __launch_bounds__(NTG + 32, 1) rho_mixed_kernel(const __grid_constant__ Params P)
 {
     __shared__ MolDesc mol[1];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
     if (threadIdx.x < sizeof(MolDesc) / 16) ((uint4*)mol)[threadIdx.x] = ((const uint4*)&P.D)[threadIdx.x];
     const uint32_t tm_cols = tmem_cols_for(P.D.npad);
-    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, mol, tm_cols);
+    CtaState S = cta_setup<NTG + 32, NTG>(smem, mol, tm_cols);
     TileFeed F;
     F.counter = P.counter;
     F.ntiles = P.D.ntiles;
     F.descs = nullptr;
     F.nmol = 1;
     F.grab = 1;
-    if (threadIdx.x < 128 * NG)
-        gen_role<NG, false>(F, S, P.status);
+    if (threadIdx.x < NTG)
+        gen_role<NTG, PP, false>(F, S, P.status);
     else
         mma_role<false>(S, P.status);
     cta_teardown(S, tm_cols);
@@ -1046,20 +1165,20 @@ struct BatchParams {
     int* status;
 };
 
-template <int NG>
-__global__ void __launch_bounds__(128 * NG + 32, 1) rho_mixed_batch_kernel(const BatchParams P)
+template <int NTG, int PP>
+__global__ void __launch_bounds__(NTG + 32, 1) rho_mixed_batch_kernel(const BatchParams P)
 {
     __shared__ MolDesc mol[2];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    CtaState S = cta_setup<128 * NG + 32, 128 * NG>(smem, mol, 512);
+    CtaState S = cta_setup<NTG + 32, NTG>(smem, mol, 512);
     TileFeed F;
     F.counter = P.counter;
     F.ntiles = P.total_tiles;
     F.descs = P.descs;
     F.nmol = P.nmol;
     F.grab = P.grab;
-    if (threadIdx.x < 128 * NG)
-        gen_role<NG, true>(F, S, P.status);
+    if (threadIdx.x < NTG)
+        gen_role<NTG, PP, true>(F, S, P.status);
     else
         mma_role<true>(S, P.status);
     cta_teardown(S, 512);
@@ -1120,40 +1239,61 @@ using namespace okg;
 namespace okg {
 namespace mx {
 // Shared-memory attribute of every instantiation (idempotent, called at set-up).
-static cudaError_t configure_kernels()
+// Generation layouts {generation threads per CTA, grid points per generation
+// thread} with a kernel instantiation each.
+constexpr int GEN_LAYOUTS[][2] = {{256, 1}, {384, 1}, {512, 1}, {256, 2}, {384, 2}};
+constexpr int NLAYOUT = (int)(sizeof(GEN_LAYOUTS) / sizeof(GEN_LAYOUTS[0]));
+
+constexpr int LAYOUT_DEFAULT = 1;  // 384 generation threads, one point each
+
+inline int layout_index(int threads, int points)
 {
-    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < NLAYOUT; ++i)
+        if (GEN_LAYOUTS[i][0] == threads && GEN_LAYOUTS[i][1] == points) return i;
+    return -1;
+}
+
+template <int NTG, int PP>
+static cudaError_t configure_one()
+{
     const int sm = (int)SMEM_BYTES;
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(rho_mixed_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(rho_mixed_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(rho_mixed_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaError_t e = cudaFuncSetAttribute(rho_mixed_kernel<NTG, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<NTG, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     return e;
 }
 
-static void launch_single(int ng, unsigned grid, cudaStream_t st, const Params& P)
+// Shared-memory attribute of every instantiation (idempotent, called at set-up).
+static cudaError_t configure_kernels()
 {
-    if (ng == 3)
-        rho_mixed_kernel<3><<<grid, 416, SMEM_BYTES, st>>>(P);
-    else if (ng == 4)
-        rho_mixed_kernel<4><<<grid, 544, SMEM_BYTES, st>>>(P);
-    else
-        rho_mixed_kernel<2><<<grid, 288, SMEM_BYTES, st>>>(P);
+    cudaError_t e = configure_one<256, 1>();
+    if (e == cudaSuccess) e = configure_one<384, 1>();
+    if (e == cudaSuccess) e = configure_one<512, 1>();
+    if (e == cudaSuccess) e = configure_one<256, 2>();
+    if (e == cudaSuccess) e = configure_one<384, 2>();
+    return e;
 }
 
-static void launch_batch(int ng, unsigned grid, cudaStream_t st, const BatchParams& P)
+static void launch_single(int layout, unsigned grid, cudaStream_t st, const Params& P)
 {
-    if (ng == 3)
-        rho_mixed_batch_kernel<3><<<grid, 416, SMEM_BYTES, st>>>(P);
-    else if (ng == 4)
-        rho_mixed_batch_kernel<4><<<grid, 544, SMEM_BYTES, st>>>(P);
-    else
-        rho_mixed_batch_kernel<2><<<grid, 288, SMEM_BYTES, st>>>(P);
+    switch (layout) {
+    case 0: rho_mixed_kernel<256, 1><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
+    case 2: rho_mixed_kernel<512, 1><<<grid, 512 + 32, SMEM_BYTES, st>>>(P); break;
+    case 3: rho_mixed_kernel<256, 2><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
+    case 4: rho_mixed_kernel<384, 2><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
+    default: rho_mixed_kernel<384, 1><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
+    }
+}
+
+static void launch_batch(int layout, unsigned grid, cudaStream_t st, const BatchParams& P)
+{
+    switch (layout) {
+    case 0: rho_mixed_batch_kernel<256, 1><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
+    case 2: rho_mixed_batch_kernel<512, 1><<<grid, 512 + 32, SMEM_BYTES, st>>>(P); break;
+    case 3: rho_mixed_batch_kernel<256, 2><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
+    case 4: rho_mixed_batch_kernel<384, 2><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
+    default: rho_mixed_batch_kernel<384, 1><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
+    }
 }
 }  // namespace mx
 }  // namespace okg
@@ -1168,7 +1308,7 @@ struct okg_mixed_plan {
     int* status;
     int sm_count;
     size_t smem;
-    int ngen;  // generation groups per point (threads per CTA = 128 x ngen)
+    int layout;  // index into GEN_LAYOUTS (generation threads, points per thread)
 };
 
 extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_max, okg_mixed_plan** out);
@@ -1213,7 +1353,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     cudaMemset(p->status, 0, sizeof(int));
     p->sm_count = sms;
     p->smem = mx::SMEM_BYTES;
-    p->ngen = mx::NG_DEFAULT;
+    p->layout = mx::LAYOUT_DEFAULT;
     e = mx::configure_kernels();
     if (e != cudaSuccess) {
         cudaFree(p->block);
@@ -1228,7 +1368,17 @@ extern "C" int okg_mixed_plan_set_threads(okg_mixed_plan* p, int threads)
 {
     if (!p || (threads != 256 && threads != 384 && threads != 512))
         return set_error(OKG_ERR_ARG, "okg_mixed_plan_set_threads: threads must be 256, 384 or 512");
-    p->ngen = threads / 128;
+    p->layout = mx::layout_index(threads, 1);
+    return OKG_OK;
+}
+
+extern "C" int okg_mixed_plan_set_generation(okg_mixed_plan* p, int threads, int points_per_thread)
+{
+    const int l = mx::layout_index(threads, points_per_thread);
+    if (!p || l < 0)
+        return set_error(OKG_ERR_ARG, "okg_mixed_plan_set_generation: (threads, points) must be (256|384|512, 1) or "
+                                      "(256|384, 2)");
+    p->layout = l;
     return OKG_OK;
 }
 
@@ -1281,7 +1431,7 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
         if (e0 != cudaSuccess) return cuda_status(e0, "okg_rho_mixed: counter reset");
     }
     const long long grid = P.D.ntiles < p->sm_count ? P.D.ntiles : p->sm_count;
-    mx::launch_single(p->ngen, (unsigned)grid, (cudaStream_t)stream, P);
+    mx::launch_single(p->layout, (unsigned)grid, (cudaStream_t)stream, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
 }
 
@@ -1296,7 +1446,7 @@ struct okg_batch {
     int grab;
     int ctas;
     size_t smem;
-    int ngen;
+    int layout;
 };
 
 extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* grids, double* const* d_rho,
@@ -1355,7 +1505,7 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
     b->grab = 1;
     b->ctas = b->sm_count;
     b->smem = mx::SMEM_BYTES;
-    b->ngen = mx::NG_DEFAULT;
+    b->layout = mx::LAYOUT_DEFAULT;
     e = mx::configure_kernels();
     if (e != cudaSuccess) {
         cudaFree(b->block);
@@ -1382,7 +1532,17 @@ extern "C" int okg_batch_set_schedule(okg_batch* b, int grab, int ctas, int thre
         return set_error(OKG_ERR_ARG, "okg_batch_set_schedule: threads must be 256, 384 or 512");
     b->grab = grab;
     b->ctas = ctas;
-    b->ngen = threads / 128;
+    b->layout = mx::layout_index(threads, 1);
+    return OKG_OK;
+}
+
+extern "C" int okg_batch_set_generation(okg_batch* b, int threads, int points_per_thread)
+{
+    const int l = mx::layout_index(threads, points_per_thread);
+    if (!b || l < 0)
+        return set_error(OKG_ERR_ARG, "okg_batch_set_generation: (threads, points) must be (256|384|512, 1) or "
+                                      "(256|384, 2)");
+    b->layout = l;
     return OKG_OK;
 }
 
@@ -1408,7 +1568,7 @@ extern "C" int okg_batch_run(okg_batch* b, okg_stream stream)
     P.counter = b->d_counter;
     P.status = b->d_status;
     const long long grid = b->total_tiles < b->ctas ? b->total_tiles : b->ctas;
-    mx::launch_batch(b->ngen, (unsigned)grid, st, P);
+    mx::launch_batch(b->layout, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_batch_run launch");
 }
 
@@ -1559,6 +1719,6 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     e = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: counter reset");
     const long long grid = P.D.ntiles < nd->sm_count ? P.D.ntiles : nd->sm_count;
-    launch_single(NG_DEFAULT, (unsigned)grid, st, P);
+    launch_single(LAYOUT_DEFAULT, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed_noalloc launch");
 }

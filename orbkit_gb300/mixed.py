@@ -30,6 +30,7 @@ _SIGS = {
                                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "okg_mixed_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "okg_mixed_plan_set_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "okg_mixed_plan_set_generation": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }
 
 
@@ -64,8 +65,13 @@ class MixedPlan:
             self.set_threads(threads)
 
     def set_threads(self, threads):
-        """Threads per CTA of the mixed kernel: 256, 384 or 512."""
+        """AO-generation threads per CTA of the mixed kernel: 256, 384 or 512 (one point each)."""
         _lib.check(self._L.okg_mixed_plan_set_threads(self._h, int(threads)))
+
+    def set_generation(self, threads, points_per_thread):
+        """Generation threads per CTA and grid points per generation thread:
+        (256|384|512, 1) or (256|384, 2)."""
+        _lib.check(self._L.okg_mixed_plan_set_generation(self._h, int(threads), int(points_per_thread)))
 
     @property
     def handle(self):
