@@ -248,6 +248,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     ev.check()
     err = mixed.error_report(rho.cpu().numpy(), grad.cpu().numpy(), r64.cpu().numpy(), g64.cpu().numpy())
+    # the tensor-core kernel alone at the points the FP64 recomputation replaces
+    near = mixed.cusp_points_regular(qc.geo_spec, gx, gy, gz, ev.cusp_radius)
+    plan.rho(gd, rho, grad, npts)
+    torch.cuda.synchronize()
+    err_near = mixed.error_report(rho.cpu().numpy()[near], grad.cpu().numpy()[:, near], r64.cpu().numpy()[near],
+                                  g64.cpu().numpy()[:, near]) if len(near) else None
 
     fp64_ms, _, _ = timed(step_fp64, 2, 1)
 
@@ -322,6 +328,10 @@ def run_ours(args):
             "max_rel_err": {"rho_max_rel": err["rho_max_rel"], "rho_floor": err["floor"],
                             "rho_max_abs": err["rho_max_abs"], "grad_max_rel": err["grad_max_rel"],
                             "against": "FP64 GPU path (1e-12 of the oracle)"},
+            "near_nuclei_tensor_core_err": None if err_near is None else {
+                "points": int(len(near)), "rho_max_rel": err_near["rho_max_rel"],
+                "grad_max_rel": err_near["grad_max_rel"],
+                "note": "the tensor-core kernel alone at the points recomputed in FP64"},
             "fp64_path": {"value": world * npts / (fp64_ms * 1e-3), "ms_per_step": fp64_ms,
                           "fp64_fma_per_s_contraction": fp64_path_fma_rate},
             "mixed_over_fp64": fp64_ms / ms,
@@ -486,14 +496,24 @@ def run_workload(args):
         d = synthetic.batch()
         mols = [(m["qc"], m["points"]) for m in d["molecules"]]
         npts = sum(pp.shape[1] for _, pp in mols)
+        from orbkit_gb300 import mixed
         ev = BatchEvaluator(mols, cusp_radius=0.0, tune=True)
         graph = ev.capture()
         ms = _time_ms(graph.replay, args.steps, args.warmup)
         ev.check()
+        # the same batch with the points within CUSP_RADIUS of a nucleus recomputed by
+        # the FP64 path (a third of the points of these atom-centred grids)
+        ev.cusp_radius = mixed.CUSP_RADIUS
+        graph1 = ev.capture()
+        ms1 = _time_ms(graph1.replay, max(2, args.steps // 5), 1)
+        ev.check()
+        ncusp = sum(len(c[0]) for c in ev._cusp)
         out.update({"value": npts / (ms * 1e-3), "ms_per_step": ms,
                     "config": {"workload": "batch: 256 molecules, 3-60 atoms, atom-centred point sets",
                                "npts": npts, "molecules": len(mols), "tiles": ev.tiles(), "schedule": ev.schedule,
-                               "launch": "CUDA graph replay of one persistent kernel", "cusp_radius": 0.0}})
+                               "launch": "CUDA graph replay of one persistent kernel", "cusp_radius": 0.0,
+                               "with_fp64_cusp_points": {"cusp_radius": mixed.CUSP_RADIUS, "cusp_points": ncusp,
+                                                         "value": npts / (ms1 * 1e-3), "ms_per_step": ms1}}})
     print(json.dumps(out))
 
 

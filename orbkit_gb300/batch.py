@@ -6,8 +6,9 @@ and builds one okg_batch: all 128-point tiles of all molecules, handed out by a
 device counter to one persistent CTA per SM.  ``run()`` is a counter reset plus
 one kernel launch (plus the FP64 recomputation of cusp points when
 ``cusp_radius > 0``); ``capture()`` records it in a CUDA graph; the schedule
-(MMA N tile per MO pass, tiles per counter grab, molecule order) comes from the
-autotuner (orbkit_gb300.autotune), measured once per size bucket.
+(MMA N tile per MO pass, tiles per counter grab, molecule order, generation
+threads and points per thread) comes from the autotuner (orbkit_gb300.autotune),
+measured once per size bucket.
 """
 import ctypes
 
@@ -28,6 +29,7 @@ _SIGS = {
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "okg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "okg_batch_set_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "okg_batch_set_generation": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "okg_batch_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "okg_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "okg_batch_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
@@ -36,7 +38,8 @@ _SIGS = {
 N_TILES = (32, 64)
 GRABS = (1, 4)
 ORDERS = ("given", "largest_first")
-THREADS = (256, 384, 512)
+# (generation threads per CTA, grid points per generation thread)
+LAYOUTS = ((256, 1), (384, 1), (512, 1), (256, 2))
 
 
 def _L():
@@ -88,7 +91,7 @@ class BatchEvaluator:
         self._batch = None
         self._cusp = None
         if schedule is None:
-            schedule = self.autotune() if tune else {"n_max": 64, "grab": 1, "order": "given", "threads": 256}
+            schedule = self.autotune() if tune else {"n_max": 64, "grab": 1, "order": "given", "layout": (384, 1)}
         self.set_schedule(schedule)
 
     # ------------------------------------------------------------- schedule
@@ -127,7 +130,9 @@ class BatchEvaluator:
                                             ctypes.byref(h)))
         self._batch = h
         sms = __import__("torch").cuda.get_device_properties(self.device).multi_processor_count
-        _lib.check(self._L.okg_batch_set_schedule(h, sch["grab"], sms, sch.get("threads", 256)))
+        threads, points = sch.get("layout", (sch.get("threads", 384), 1))
+        _lib.check(self._L.okg_batch_set_schedule(h, sch["grab"], sms, 384))
+        _lib.check(self._L.okg_batch_set_generation(h, int(threads), int(points)))
         self.schedule = dict(sch)
 
     def tiles(self):
@@ -140,8 +145,8 @@ class BatchEvaluator:
         key = "batch-" + autotune.bucket(nmol=len(self.mols), pts=self.npts,
                                          nao=max(m["basis"].ncart for m in self.mols),
                                          nmo=max(len(m["occ"]) for m in self.mols))
-        cands = [{"n_max": n, "grab": g, "order": o, "threads": t}
-                 for n in N_TILES for g in GRABS for o in ORDERS for t in THREADS]
+        cands = [{"n_max": n, "grab": g, "order": o, "layout": lt}
+                 for n in N_TILES for g in GRABS for o in ORDERS for lt in LAYOUTS]
 
         def measure(c):
             self.set_schedule(c)

@@ -72,7 +72,8 @@ __global__ void __launch_bounds__(128) ao_eval_kernel(BasisDev B, Grid g, DrvLis
 }
 
 // ------------------------------------------------------------- fused kernels
-// CTA = P points x G MO groups (256 threads).  For each chunk of shells, every
+// CTA = FP points x FG MO groups (64 x 4 = 256 threads; 8 x 16 for small point
+// sets).  For each chunk of shells, every
 // group evaluates a share of the chunk's shells for its point into shared memory
 // (AO_s[channel][row][point], NCH channels = the first NCH of value, d/dx, d/dy,
 // d/dz, xx, yy, zz, xy, xz, yz); the chunk's MO coefficients are staged in C_s;
@@ -118,9 +119,10 @@ __host__ __device__ inline void second_pair(int code, int& a, int& b)
     }
 }
 
-template <int NCH, int MB, bool MO_OUT>
-__global__ void __launch_bounds__(FT) fused64_kernel(BasisDev B, Grid g, FusedArgs A)
+template <int NCH, int MB, bool MO_OUT, int FP = okg::FP, int FG = okg::FG>
+__global__ void __launch_bounds__(FP * FG) fused64_kernel(BasisDev B, Grid g, FusedArgs A)
 {
+    constexpr int FT = FP * FG;
     extern __shared__ double smem[];
     double* AO_s = smem;                          // NCH x KC x FP
     double* C_s = smem + NCH * OKG_KC * FP;       // FG*MB x KC
@@ -247,22 +249,37 @@ __global__ void __launch_bounds__(FT) fused64_kernel(BasisDev B, Grid g, FusedAr
     }
 }
 
-template <int NCH, int MB, bool MO_OUT>
+template <int NCH, int MB, bool MO_OUT, int FPx = FP, int FGx = FG>
 static int launch_fused(const okg_basis* b, const Grid& g, const FusedArgs& A, cudaStream_t st)
 {
-    const size_t smem_main = sizeof(double) * ((size_t)NCH * OKG_KC * FP + (size_t)FG * MB * OKG_KC);
-    const size_t smem_red = sizeof(double) * FG * 11 * FP;
+    const size_t smem_main = sizeof(double) * ((size_t)NCH * OKG_KC * FPx + (size_t)FGx * MB * OKG_KC);
+    const size_t smem_red = sizeof(double) * FGx * 11 * FPx;
     const size_t smem = smem_main > smem_red ? smem_main : smem_red;
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(fused64_kernel<NCH, MB, MO_OUT>,
+        cudaError_t e = cudaFuncSetAttribute(fused64_kernel<NCH, MB, MO_OUT, FPx, FGx>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return cuda_status(e, "fused64: smem attribute");
         configured = true;
     }
-    const long long nblk = (g.npts + FP - 1) / FP;
-    fused64_kernel<NCH, MB, MO_OUT><<<(unsigned)nblk, FT, smem, st>>>(b->dev, g, A);
+    const long long nblk = (g.npts + FPx - 1) / FPx;
+    fused64_kernel<NCH, MB, MO_OUT, FPx, FGx><<<(unsigned)nblk, FPx * FGx, smem, st>>>(b->dev, g, A);
     return cuda_status(cudaGetLastError(), "fused64 launch");
+}
+
+// Small point sets -- fewer than one wave of the 64-point CTAs, e.g. the FP64
+// recomputation of the points near nuclei on the mixed path -- use CTAs of 8
+// points x 16 MO groups: the same kernel and per-point arithmetic, 8x as many
+// CTAs, every lane busy in the AO and in the MO part (measured faster than 2 x 64
+// on 678 points: more CTAs restage the coefficients more often).
+constexpr long long FEW_MAX_POINTS = 152 * FP;
+
+static int dispatch_few(const okg_basis* b, const Grid& g, const FusedArgs& A, unsigned need, cudaStream_t st)
+{
+    if ((need & ~1u) == 0) return launch_fused<1, 8, false, 8, 16>(b, g, A, st);
+    if ((need & ~0xFu) == 0) return launch_fused<4, 4, false, 8, 16>(b, g, A, st);
+    if ((need & ~0x7Fu) == 0) return launch_fused<7, 3, false, 8, 16>(b, g, A, st);
+    return launch_fused<10, 2, false, 8, 16>(b, g, A, st);
 }
 
 template <bool MO_OUT>
@@ -387,5 +404,7 @@ extern "C" int okg_rho(const okg_basis* b, const okg_grid* grid, int nmo, const 
     A.dout = d_drho;
     A.mo_norm = d_mo_norm;
     A.ld = ld;
+    // (the MO-norm sums reduce over warps of one MO group: 64-point CTAs only)
+    if (g.npts <= FEW_MAX_POINTS && !A.mo_norm) return dispatch_few(b, g, A, need, (cudaStream_t)stream);
     return dispatch_fused<false>(b, g, A, need, (cudaStream_t)stream);
 }

@@ -148,54 +148,45 @@ class MixedEvaluator:
             _lib.check(p._L.okg_mixed_set_coeffs(p.handle, _lib.ptr(p.C), _lib.ptr(p.occ), _lib.stream_handle(stream)))
 
     def evaluate_device(self, g, rho=None, grad=None):
-        """Run on a _DeviceGrid; returns device tensors (rho, grad).  The FP64
-        recomputation of the cusp points runs on a side stream concurrently with
-        the mixed kernel and is scattered into the outputs afterwards."""
+        """Run on a _DeviceGrid; returns device tensors (rho, grad).  The points
+        within the cusp radius of a nucleus are then recomputed by the FP64 path
+        (its small-point CTA shape) and scattered into the outputs, on the same
+        stream."""
         import torch
         n = g.npts
         if rho is None:
             rho = torch.empty(n, dtype=torch.float64, device=self.device)
             grad = torch.empty((3, n), dtype=torch.float64, device=self.device)
         gd, keep = g.slice(0, n)
-        fix = None
-        if self.cusp_radius and self.cusp_radius > 0:
-            fix = self._cusp_launch(g)
         self.plan.rho(gd, rho, grad, n)
-        if fix is not None:
-            idx, r, dr, ev = fix
-            torch.cuda.current_stream().wait_event(ev)
-            rho.index_copy_(0, idx, r)
-            grad.index_copy_(1, idx, dr)
+        if self.cusp_radius and self.cusp_radius > 0:
+            self._cusp_fix(g, rho, grad)
         return rho, grad
 
-    def _cusp_launch(self, g):
+    def _cusp_fix(self, g, rho, grad):
         import torch
-        key = (tuple((v.__array_interface__["data"][0], v.shape) for v in g.host), g.regular, self.cusp_radius,
-               self.geo.tobytes())
+        # cached per regular grid (its axes) or per vector-grid object (held here, so
+        # its identity is not reused), and per geometry and radius
+        key = (self.cusp_radius, self.geo.tobytes(),
+               tuple(numpy.ascontiguousarray(v).tobytes() for v in g.host) if g.regular else id(g))
         if getattr(self, "_cusp_key", None) != key:
+            self._cusp_grid = g
             self._cusp_key = key
-            self._cusp = cusp_points(self.geo, g, self.cusp_radius, self.device)
-            self._side = torch.cuda.Stream(device=self.device)
-        idx, pts = self._cusp
-        m = len(idx)
-        if m == 0:
-            return None
-        main = torch.cuda.current_stream()
-        self._side.wait_stream(main)
-        with torch.cuda.stream(self._side):
+            idx, pts = cusp_points(self.geo, g, self.cusp_radius, self.device)
+            m = len(idx)
             r = torch.empty(m, dtype=torch.float64, device=self.device)
             dr = torch.empty((3, m), dtype=torch.float64, device=self.device)
             gd = _lib.OkgGrid(pts[0].data_ptr(), pts[1].data_ptr(), pts[2].data_ptr(), m, 0, 0, 0, 0, 0)
-            L = _lib.load()
-            p = self.plan
-            _lib.check(L.okg_rho(p.basis.handle, gd, p.nmo, _lib.ptr(p.C), _lib.ptr(p.occ), 3,
-                                 _lib.int_array([1, 2, 3]), 1, _lib.ptr(r), _lib.ptr(dr), m, None,
-                                 _lib.stream_handle(self._side)))
-            ev = torch.cuda.Event()
-            ev.record(self._side)
-        r.record_stream(main)
-        dr.record_stream(main)
-        return idx, r, dr, ev
+            self._cusp = (idx, pts, r, dr, gd, _lib.int_array([1, 2, 3]))
+        idx, pts, r, dr, gd, codes = self._cusp
+        m = len(idx)
+        if m == 0:
+            return
+        p = self.plan
+        _lib.check(_lib.load().okg_rho(p.basis.handle, gd, p.nmo, _lib.ptr(p.C), _lib.ptr(p.occ), 3, codes, 1,
+                                       _lib.ptr(r), _lib.ptr(dr), m, None, _lib.stream_handle()))
+        rho.index_copy_(0, idx, r)
+        grad.index_copy_(1, idx, dr)
 
     def evaluate(self, x, y, z, is_vector, out=None):
         """Host grid in, host (rho, grad) out.  `out` may hold preallocated (pinned)

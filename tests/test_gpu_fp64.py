@@ -146,6 +146,30 @@ def test_many_mos_multiple_passes(core):
     assert_fp64_close(m, mref, "mo")
 
 
+def test_few_points_kernel(core):
+    """Small point sets (one CTA per point): 260 MOs (up to three MOs per thread), a
+    spherical basis with f shells (267 AOs), rho alone, rho with one derivative and with
+    x, y, z."""
+    import okref
+    from orbkit_gb300 import synthetic
+    rng = numpy.random.default_rng(17)
+    el = ["C", "O", "N", "H", "C", "H", "O", "C", "H", "N", "C", "C", "O", "N", "C"]
+    geo = synthetic.random_geometry(rng, len(el), 11.0)
+    ao = synthetic.build_basis(rng, el, with_f=True, spherical=True)
+    mo = synthetic.build_mos(rng, geo, ao, 260)
+    qc = synthetic.make_qc(geo, el, ao, mo)
+    p = rng.uniform(-6, 6, (3, 300))
+    p[:, :3] = numpy.asarray(qc.geo_spec)[:3].T
+    for drv in (None, ["y"], ["x", "y", "z"]):
+        out = core.rho_compute_no_slice(qc, drv=drv, x=p[0], y=p[1], z=p[2], is_vector=True)
+        ref = okref.rho_threads(qc, *p, drv=drv, slice_length=64, nthreads=4)
+        if drv is None:
+            assert_fp64_close(out, ref if not isinstance(ref, tuple) else ref[0], "rho")
+        else:
+            assert_fp64_close(out[0], ref[0], "rho %s" % drv)
+            assert_fp64_close(out[1], ref[1], "drho %s" % drv)
+
+
 def test_exact_mixed_derivatives(core):
     """exact_mixed=True gives the true d2/dxdy (checked by central differences of d/dx)."""
     from orbkit_gb300 import synthetic

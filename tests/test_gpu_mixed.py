@@ -111,6 +111,31 @@ def test_mixed_spherical_f_many_mos(mixed):
     _check(mixed, r, g, ro, go, "spherical f, 100 MOs")
 
 
+@pytest.mark.parametrize("layout", [(256, 1), (512, 1), (256, 2), (384, 2)])
+def test_mixed_generation_layouts(mixed, layout):
+    """Every generation layout (threads per CTA, points per thread) on a spherical f basis,
+    a brick-tiled full grid and ragged vector point sets."""
+    import okref
+    from orbkit_gb300 import synthetic
+    rng = numpy.random.default_rng(31)
+    el = ["C", "O", "H", "N", "H", "C"]
+    geo = synthetic.random_geometry(rng, len(el), 7.0)
+    ao = synthetic.build_basis(rng, el, with_f=True, spherical=True)
+    mo = synthetic.build_mos(rng, geo, ao, 30)
+    qc = synthetic.make_qc(geo, el, ao, mo)
+    ev = mixed.MixedEvaluator(qc)
+    ev.plan.set_generation(*layout)
+    g = numpy.linspace(-4.0, 4.0, 21)
+    r, gr = ev.evaluate(g, g[:13], g[:9], False)
+    ro, go = okref.rho_threads(qc, *okref.grid2vector(g, g[:13], g[:9]), drv=["x", "y", "z"], slice_length=256)
+    _check(mixed, r, gr, ro, go, "grid %s" % (layout,))
+    for n in (1, 129, 700):
+        p = rng.uniform(-5, 5, (3, n))
+        r, gr = ev.evaluate(p[0], p[1], p[2], True)
+        ro, go = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=128, nthreads=2)
+        _check(mixed, r, gr, ro, go, "n=%d %s" % (n, layout))
+
+
 def test_mixed_through_drop_in_api(mixed):
     """core.rho_compute(..., precision='mixed') routes rho / grad rho to the tensor-core path."""
     from helpers import load_golden
