@@ -392,6 +392,13 @@ __device__ __forceinline__ void gen_sync()
     asm volatile("bar.sync 1, %0;" ::"r"(NTG) : "memory");
 }
 
+// K-steps (16 columns each) of a kept chunk that hold a kept column: the MMAs of a
+// K-step whose columns are all screened are not issued.
+__device__ __forceinline__ int ksteps_of(unsigned km)
+{
+    return ((km & 0xFFFFu) != 0u) + ((km >> 16) != 0u);
+}
+
 // Next chunk after c (in chunk order) with a kept column, or -1.
 __device__ __forceinline__ int next_kept(const unsigned* km, int nmchunk, int c)
 {
@@ -692,7 +699,7 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaSta
 // FP32 (exact products by FMA, two-sum accumulation, about 44 bits) and added to
 // the FP64 accumulators.
 template <int E>
-__device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nchunks, const CtaState& S,
+__device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nksteps, const CtaState& S,
                                              uint32_t& accseq, double (&acc)[4], int* status)
 {
     const int warp = threadIdx.x >> 5;
@@ -708,7 +715,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nch
         const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
         const float2* occf = D.occf + pass * npad;
         const float2* occ2f = D.occf + (D.npass + pass) * npad;
-        const int nlead = 2 * nchunks < 4 ? 2 * nchunks : 4;  // leading accumulators written in this job
+        const int nlead = nksteps < 4 ? nksteps : 4;  // leading accumulators written in this job
         int mo_end = D.nmo - pass * npad;
         mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
         for (int m0 = 0; m0 < mo_end; m0 += 8) {
@@ -770,7 +777,7 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
     int gpass = 0;
     AtomRun<P> ar;
     int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
-    int nch = 0;
+    int nch = 0, nks = 0;  // chunks and K-steps issued in the current job
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     for (;;) {
         const MolDesc& Dg = S.mol[BATCH ? (ord & 1) : 0];
@@ -781,6 +788,7 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
             while (c >= 0) {
                 gen_chunk<NTG, P>(B, c, S, seq, ar, chmask, gp, status);
                 ++nch;
+                nks += ksteps_of(km[c]);
                 c = next_kept(km, B.nmchunk, c);
             }
         }
@@ -794,7 +802,7 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
             npass_next = 0;
             more = fetch_and_screen<NTG, P, BATCH>(F, S, ord_next, gnext, gend, p_next, valid_next, gp, status) >= 0;
         }
-        int c_next = -1, nch_next = 0;
+        int c_next = -1, nch_next = 0, nks_next = 0;
         if (more) {
             const MolDesc& Dn = S.mol[BATCH ? (ord_next & 1) : 0];
             const unsigned* kmn = S.kmask + (ord_next & 1) * MAX_CHUNKS;
@@ -803,11 +811,12 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
             if (c_next >= 0) {
                 gen_chunk<NTG, P>(Dn.B, c_next, S, seq, ar, Dn.want_grad ? 0xFu : 0x1u, gp, status);
                 ++nch_next;
+                nks_next += ksteps_of(kmn[c_next]);
                 c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
             }
         }
         // the current job's epilogue (nothing to read if none of its chunks reached the tile)
-        if (nch > 0) gen_epilogue<E>(Dg, gpass, nch, S, accseq, acc, status);
+        if (nch > 0) gen_epilogue<E>(Dg, gpass, nks, S, accseq, acc, status);
         if (gpass == Dg.npass - 1) {
             if (valid && !*S.abort_flag) {
                 if (0 % E == h) Dg.rho[p] = acc[0];
@@ -827,6 +836,7 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
         valid = valid_next;
         c = c_next;
         nch = nch_next;
+        nks = nks_next;
     }
 }
 
@@ -950,6 +960,7 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
             tc_fence_after();
             const int nch = cur.nch;
             const int pf = nch > 2 ? 1 : nch - 1;  // channel after which the next B block is requested
+            const bool kon[2] = {(cur.km & 0xFFFFu) != 0u, (cur.km >> 16) != 0u};
             if (!*S.abort_flag) {
                 const uint32_t idesc = idesc_bf16(M, npad);
                 const uint32_t bpart16 = (uint32_t)(npad * ROWB) >> 4;
@@ -959,7 +970,8 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
                 for (int ch = 0; ch < nch; ++ch) {
 #pragma unroll
                     for (int k = 0; k < KC / 16; ++k) {
-                        const int ks = kq + k;
+                        if (!kon[k]) continue;  // all 16 columns screened
+                        const int ks = kq + (k == 1 && kon[0]);
                         // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
                         const int pa[6] = {0, 0, 1, 0, 1, 2};
                         const int pb[6] = {0, 1, 0, 2, 1, 0};
@@ -998,7 +1010,7 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
         }
         __syncwarp();
         ++seq;
-        kq += KC / 16;
+        kq += ksteps_of(cur.km);
         if (!in_tile || nxt.pass != cur.pass) {
             ++accseq;
             kq = 0;
