@@ -429,8 +429,8 @@ struct GenPts {
 
 template <int NTG, int P, bool BATCH>
 __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const CtaState& S, uint32_t ord,
-                                                      long long& gnext, long long& gend, long long& p, bool& valid,
-                                                      GenPts<P>& gp, int* status)
+                                                      long long& gnext, long long& gend, long long& gpend,
+                                                      long long& p, bool& valid, GenPts<P>& gp, int* status)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int b = ord & 1;
@@ -441,17 +441,23 @@ __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const C
     if (warp == 0) {
         long long t = -1;
         int mol = 0;
+        // the counter increment for the following tile (or range) is issued one
+        // fetch ahead (gpend, thread 0 only), so its round trip overlaps a tile
         if (lane == 0 && !*S.abort_flag) {
             if (!BATCH) {
-                t = (long long)atomicAdd(F.counter, 1ull);
+                t = gpend >= 0 ? gpend : (long long)atomicAdd(F.counter, 1ull);
+                gpend = (long long)atomicAdd(F.counter, 1ull);
                 if (t >= F.ntiles) t = -1;
             } else {
                 if (gnext >= gend) {
-                    gnext = (long long)atomicAdd(F.counter, (unsigned long long)F.grab);
+                    gnext = gpend >= 0 ? gpend : (long long)atomicAdd(F.counter, (unsigned long long)F.grab);
+                    gpend = -1;
                     gend = gnext + F.grab < F.ntiles ? gnext + F.grab : F.ntiles;
                 }
                 if (gnext < gend) {
                     t = gnext++;
+                    if (gnext == gend && gend < F.ntiles)
+                        gpend = (long long)atomicAdd(F.counter, (unsigned long long)F.grab);
                     int lo = 0, hi = F.nmol - 1;
                     while (lo < hi) {
                         const int mid = (lo + hi + 1) >> 1;
@@ -769,11 +775,11 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
     const int warp = threadIdx.x >> 5;
     const int h = warp >> 2;
     uint32_t seq = 0, accseq = 0, ord = 0;
-    long long gnext = 0, gend = 0;
+    long long gnext = 0, gend = 0, gpend = -1;
     long long p = 0;
     bool valid = false;
     GenPts<P> gp;
-    if (fetch_and_screen<NTG, P, BATCH>(F, S, ord, gnext, gend, p, valid, gp, status) < 0) return;
+    if (fetch_and_screen<NTG, P, BATCH>(F, S, ord, gnext, gend, gpend, p, valid, gp, status) < 0) return;
     int gpass = 0;
     AtomRun<P> ar;
     int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
@@ -800,7 +806,8 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
         if (npass_next == Dg.npass) {
             ord_next = ord + 1;
             npass_next = 0;
-            more = fetch_and_screen<NTG, P, BATCH>(F, S, ord_next, gnext, gend, p_next, valid_next, gp, status) >= 0;
+            more = fetch_and_screen<NTG, P, BATCH>(F, S, ord_next, gnext, gend, gpend, p_next, valid_next, gp,
+                                                   status) >= 0;
         }
         int c_next = -1, nch_next = 0, nks_next = 0;
         if (more) {
