@@ -204,3 +204,31 @@ def test_c_abi_errors(core):
     gr = _lib.OkgGrid(x.data_ptr(), x.data_ptr(), x.data_ptr(), 10, 995, 10, 10, 10, 1)
     assert L.okg_eval_ao(b.handle, ctypes.byref(gr), 1, _lib.int_array([0]), 0, _lib.ptr(out), 10, None) == -1
     torch.cuda.synchronize()
+
+
+def test_mo_matrix_and_transition_flux(core):
+    """core.calc_mo_matrix (MO_a x dMO_b products, orbkit/core.py:841-941) and
+    extras.calc_jmo (orbkit/extras.py:441-492) on the module grid, against the
+    oracle's MO grids."""
+    import okref
+    from orbkit_gb300 import extras, grid, synthetic
+    qc = synthetic.small()["qc"]
+    x = numpy.linspace(-3.0, 3.0, 7)
+    y = numpy.linspace(-2.5, 2.5, 6)
+    z = numpy.linspace(-2.0, 2.0, 5)
+    grid.set_grid(x, y, z, is_vector=False)
+    drv = ["x", "y", "z"]
+    mm = core.calc_mo_matrix(qc, drv=drv)
+    mo = okref.rho_compute_no_slice(qc, calc_mo=True, drv=[None] + drv, x=x, y=y, z=z, is_vector=False)
+    nmo = mo.shape[1]
+    assert mm.shape == (3, nmo, nmo) + (7, 6, 5)
+    ref = numpy.einsum("aigkl,dbgkl->daibgkl", mo[:1], mo[1:])[:, 0]
+    assert_fp64_close(mm, ref, "mo matrix")
+    pairs = [(0, 1), (2, 1), (3, 3)]
+    jmo = extras.calc_jmo(qc, pairs, drv=drv)
+    assert jmo.shape == (3, 3, 7, 6, 5)
+    for n, (i, j) in enumerate(pairs):
+        expect = -0.5 * (mo[0, i] * mo[1:, j] - mo[0, j] * mo[1:, i])
+        assert_fp64_close(jmo[:, n], expect, "jmo %d %d" % (i, j))
+    assert numpy.abs(jmo[:, 2]).max() == 0.0
+    grid.reset_grid()
