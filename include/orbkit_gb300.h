@@ -206,6 +206,28 @@ int okg_rho_mixed_noalloc(const okg_basis* basis, const okg_grid* grid, int nmo,
                           const double* d_occ, int want_grad, double* d_rho, double* d_grad, int64_t ld,
                           int* d_status, okg_stream stream);
 
+/* ------------------------------------------------------------------- detCI
+ * CI (transition) densities and flux densities on a grid from MO grids d_mo
+ * (nmo x ld, points contiguous: orbkit's molist) and, for the fluxes, their x, y, z
+ * derivatives d_drv (3 x nmo x ld: orbkit's molistdrv).  The terms come from
+ * orbkit's determinant comparison (orbkit/detci/occ_check.py): "zero" terms
+ * (coefficient d_zcoef[t], orbital d_zidx[t]) and single-excitation terms
+ * (coefficient d_scoef[t], orbitals d_spair[2t], d_spair[2t+1]), all on the device.
+ * Terms are summed in the given order with orbkit's rounding of every product and
+ * sum (no FMA contraction). */
+/* rho[p] = sum_t zc[t] MO_zi[t](p)^2 + sum_t sc[t] MO_a(p) MO_b(p):
+ * replaces orbkit/detci/cy_ci.pyx:70-96 (get_rho) behind detci.ci_core.rho. */
+int okg_ci_rho(int64_t npts, const double* d_mo, int64_t ld, int nz, const double* d_zcoef, const int* d_zidx,
+               int ns, const double* d_scoef, const int* d_spair, double* d_rho, okg_stream stream);
+/* j[d*npts + p] = -sum_t 0.5 sc[t] (MO_a dMO_b - MO_b dMO_a), d = x, y, z:
+ * replaces orbkit/detci/cy_ci.pyx:152-178 (get_jab) behind detci.ci_core.jab. */
+int okg_ci_jab(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld, int nmo, int ns,
+               const double* d_scoef, const int* d_spair, double* d_j, okg_stream stream);
+/* j[d*npts + p] = sum_t sc[t] MO_a dMO_b: replaces orbkit/detci/cy_ci.pyx:203-229
+ * (get_a_nabla_b) behind detci.ci_core.a_nabla_b. */
+int okg_ci_a_nabla_b(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld, int nmo, int ns,
+                     const double* d_scoef, const int* d_spair, double* d_j, okg_stream stream);
+
 /* Diagnostic (no counterpart in orbkit): measured FP64 FMA rate of the current device
  * in FMA/s, from a kernel of independent FMA chains (synchronising; allocates). */
 int okg_diag_fp64_fma_rate(long long iters, double* fma_per_s);

@@ -8,6 +8,12 @@ reference's setup.py declares at setup.py:51-75:
   orbkit.cy_core    <- orbkit/cy_core.pyx + orbkit/c_grid-based.c + orbkit/c_support.c
   orbkit.cy_overlap <- orbkit/cy_overlap.pyx + orbkit/c_non-grid-based.c + orbkit/c_support.c
 
+and the two detCI extensions (setup.py:76-95) whose grid loops the CI density and
+flux-density fixtures come from:
+
+  orbkit.detci.cy_ci        <- orbkit/detci/cy_ci.pyx
+  orbkit.detci.cy_occ_check <- orbkit/detci/cy_occ_check.pyx
+
 The sources are read where they lie (the read-only reference tree); every output
 (Cython-generated C, objects, the extension modules) goes under ``oracle/_ref/``,
 which is git-ignored.  Nothing is copied into the repository.  The reference
@@ -30,6 +36,8 @@ EXTENSIONS = [
     ("cy_grid", ["orbkit/cy_grid.pyx"], []),
     ("cy_core", ["orbkit/cy_core.pyx"], ["orbkit/c_grid-based.c", "orbkit/c_support.c"]),
     ("cy_overlap", ["orbkit/cy_overlap.pyx"], ["orbkit/c_non-grid-based.c", "orbkit/c_support.c"]),
+    ("detci.cy_ci", ["orbkit/detci/cy_ci.pyx"], []),
+    ("detci.cy_occ_check", ["orbkit/detci/cy_occ_check.pyx"], []),
 ]
 
 
@@ -41,7 +49,7 @@ def built_modules(out=OUT):
     """Paths of the built extension modules, or None when not built."""
     paths = {}
     for name, _, _ in EXTENSIONS:
-        p = os.path.join(out, "orbkit", name + ext_suffix())
+        p = os.path.join(out, "orbkit", *name.split(".")[:-1], name.split(".")[-1] + ext_suffix())
         if not os.path.exists(p):
             return None
         paths[name] = p
@@ -67,7 +75,8 @@ def build(ref_root=DEFAULT_REF, out=OUT, quiet=True):
     incs = [numpy.get_include(), sysconfig.get_paths()["include"], os.path.join(ref_root, "orbkit")]
     cflags = ["-O2", "-fPIC", "-w"] + ["-I" + i for i in incs]
     for name, pyx, csrc in EXTENSIONS:
-        target = os.path.join(mdir, name + ext_suffix())
+        target = os.path.join(mdir, *name.split(".")[:-1], name.split(".")[-1] + ext_suffix())
+        os.makedirs(os.path.dirname(target), exist_ok=True)
         srcs = [os.path.join(ref_root, p) for p in pyx + csrc]
         if os.path.exists(target) and all(os.path.getmtime(target) >= os.path.getmtime(s) for s in srcs):
             continue

@@ -450,3 +450,64 @@ def rho_threads(qc, x, y, z, drv=("x", "y", "z"), slice_length=10000, nthreads=N
     if err:
         raise MemoryError("oracle slice allocation failed")
     return rho, drho[:len(drv)]
+
+
+# ------------------------------------------------------------------- detCI
+# CI (transition) density and flux density on a grid from MO grids, restating the
+# loops of orbkit/detci/cy_ci.pyx: terms in the given order, every product and sum
+# rounded as written there (numpy float64 elementwise operations, no FMA).
+# zero = [coefficient lists, orbital lists], sing = [coefficients, orbital pairs]
+# as produced by orbkit/detci/occ_check.py.
+
+def ci_rho(zero, sing, molist):
+    """orbkit/detci/cy_ci.pyx:70-96 (get_rho) over all points."""
+    mo = numpy.asarray(molist, dtype=numpy.float64).reshape(len(molist), -1)
+    rho = numpy.zeros(mo.shape[1])
+    for cs, js in zip(zero[0], zero[1]):
+        for c, j in zip(cs, js):
+            rho += (c * mo[j]) * mo[j]
+    for c, (a, b) in zip(sing[0], sing[1]):
+        rho += (c * mo[a]) * mo[b]
+    return rho.reshape(numpy.shape(molist)[1:])
+
+
+def ci_jab(zero, sing, molist, molistdrv):
+    """orbkit/detci/cy_ci.pyx:152-178 (get_jab): -sum 0.5 c (MO_a dMO_b - MO_b dMO_a)."""
+    mo = numpy.asarray(molist, dtype=numpy.float64).reshape(len(molist), -1)
+    dr = numpy.asarray(molistdrv, dtype=numpy.float64).reshape(3, len(molist), -1)
+    j = numpy.zeros((3, mo.shape[1]))
+    for c, (a, b) in zip(sing[0], sing[1]):
+        for d in range(3):
+            j[d] -= 0.5 * (c * (mo[a] * dr[d, b] - mo[b] * dr[d, a]))
+    return j.reshape((3,) + numpy.shape(molist)[1:])
+
+
+def ci_a_nabla_b(zero, sing, molist, molistdrv):
+    """orbkit/detci/cy_ci.pyx:203-229 (get_a_nabla_b): sum c MO_a dMO_b."""
+    mo = numpy.asarray(molist, dtype=numpy.float64).reshape(len(molist), -1)
+    dr = numpy.asarray(molistdrv, dtype=numpy.float64).reshape(3, len(molist), -1)
+    j = numpy.zeros((3, mo.shape[1]))
+    for c, (a, b) in zip(sing[0], sing[1]):
+        for d in range(3):
+            j[d] += c * (mo[a] * dr[d, b])
+    return j.reshape((3,) + numpy.shape(molist)[1:])
+
+
+def ci_covered(npts, slice_length):
+    """Points orbkit's detCI drivers evaluate (orbkit/detci/ci_core.py:120-125): the
+    slices come from arange(0, npts + 1, s) with s = min(npts, slice_length), so the
+    trailing npts % s points are never evaluated and stay 0."""
+    s = int(min(npts, abs(int(slice_length))))
+    return (npts // s) * s if s > 0 else 0
+
+
+def ci_driver(fn, zero, sing, molist, *rest, slice_length=1e4):
+    """orbkit/detci/ci_core.py rho/jab/a_nabla_b: fn over all points, then the
+    driver's slicing (points beyond the last full slice left 0)."""
+    out = fn(zero, sing, molist, *rest)
+    shape = out.shape
+    flat = out.reshape(shape[:-len(numpy.shape(molist)[1:])] + (-1,)) if len(shape) > len(numpy.shape(molist)[1:]) \
+        else out.reshape(-1)
+    n = flat.shape[-1]
+    flat[..., ci_covered(n, slice_length):] = 0.0
+    return flat.reshape(shape)

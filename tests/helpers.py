@@ -52,3 +52,16 @@ def assert_fp64_close(a, b, what="", rtol=FP64_RTOL, atol_rel=FP64_ATOL_REL):
         i = numpy.unravel_index(numpy.argmax(numpy.abs(a - b) - bound), a.shape)
         raise AssertionError("%s: %d elements outside |d| <= %g|ref| + %g max|ref|; worst at %s: %r vs %r "
                              "(errors %s)" % (what, bad.sum(), rtol, atol_rel, i, a[i], b[i], rel_errors(a, b)))
+
+
+def detci_terms(d, k):
+    """(zero, sing) of state pair k of the detCI fixture, in orbkit's nested-list form."""
+    zc, zo, zl = d["zero_coef_%d" % k], d["zero_orb_%d" % k], d["zero_len_%d" % k]
+    zero = [[], []]
+    o = 0
+    for n in zl:
+        zero[0].append([float(v) for v in zc[o:o + n]])
+        zero[1].append([int(v) for v in zo[o:o + n]])
+        o += n
+    sing = [[float(v) for v in d["sing_coef_%d" % k]], [[int(a), int(b)] for a, b in d["sing_pair_%d" % k]]]
+    return zero, sing

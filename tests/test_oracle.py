@@ -147,3 +147,26 @@ def test_overlap_vs_reference(ref):
         S_ref = ai.get_ao_overlap(q.geo_spec, q.geo_spec, q.ao_spec)
         S = overlap.ao_overlap(d["qc"].geo_spec, d["qc"].ao_spec)
         numpy.testing.assert_allclose(S, S_ref, atol=1e-13)
+
+
+def test_detci_golden():
+    """CI transition densities, flux densities and their divergence of the reference's
+    H3+ FCI test (test/detci/h3+.py): MO grids from the oracle, the detCI loops
+    restated, against the reference's golden file (refdata_h3+.npz)."""
+    import okref
+    from helpers import detci_terms
+    qc, d = load_golden("h3p_detci.npz")
+    x, y, z = d["x"], d["y"], d["z"]
+    mo = okref.rho_compute_no_slice(qc, calc_mo=True, drv=[None, "x", "y", "z", "xx", "yy", "zz"], x=x, y=y, z=z,
+                                    is_vector=False)
+    # the reference test runs its drivers with slice_length=1e2 on 51 x 51 = 2601 points:
+    # its slicing leaves the last point at 0 (orbkit/detci/ci_core.py:120-125)
+    assert okref.ci_covered(51 * 51, 1e2) == 2600
+    for k in range(int(d["npairs"])):
+        zero, sing = detci_terms(d, k)
+        r = okref.ci_driver(okref.ci_rho, zero, sing, mo[0], slice_length=1e2)
+        j = okref.ci_driver(okref.ci_jab, zero, sing, mo[0], mo[1:4], slice_length=1e2)
+        nj = -okref.ci_driver(okref.ci_jab, zero, sing, mo[0], mo[4:7], slice_length=1e2).sum(axis=0)
+        for name, a, b in (("rho", r, d["rho_01"][k]), ("j", j, d["j_01"][k]), ("nabla j", nj, d["nabla_j_01"][k])):
+            assert numpy.abs(a - b).max() <= 1e-14 * numpy.abs(b).max(), (k, name, numpy.abs(a - b).max())
+        assert d["rho_01"][k].reshape(-1)[-1] == 0.0 and okref.ci_rho(zero, sing, mo[0]).reshape(-1)[-1] != 0.0
