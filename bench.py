@@ -514,7 +514,112 @@ def run_workload(args):
                                "launch": "CUDA graph replay of one persistent kernel", "cusp_radius": 0.0,
                                "with_fp64_cusp_points": {"cusp_radius": mixed.CUSP_RADIUS, "cusp_points": ncusp,
                                                          "value": npts / (ms1 * 1e-3), "ms_per_step": ms1}}})
+    elif name == "overlap":
+        out.update(_overlap_workload(args, flush))
+    elif name == "detci":
+        out.update(_detci_workload(args, flush))
     print(json.dumps(out))
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import okref
+    okref.build()
+    return okref
+
+
+def _overlap_workload(args, flush):
+    """get_ao_overlap on the 200-atom basis (2420 Cartesian AOs, spherical output):
+    S and its three ket derivatives per step."""
+    import torch
+    from orbkit_gb300 import analytical_integrals as ai, synthetic
+    qc = synthetic.large()["qc"]
+    geo = numpy.asarray(qc.geo_spec)
+    plan = ai.overlap_plan(qc.ao_spec)
+    gd = torch.tensor(geo, device="cuda")
+    outs = [torch.empty((plan.nao, plan.nao), dtype=torch.float64, device="cuda") for _ in range(4)]
+    L, h = plan._L, plan._h
+    from orbkit_gb300 import _lib
+
+    def step():
+        for d in range(4):
+            _lib.check(L.okg_ao_overlap(h, _lib.ptr(gd), _lib.ptr(gd), d, 0, _lib.ptr(outs[d]), plan.nao,
+                                        _lib.stream_handle()))
+    ms = _time_ms(step, args.steps, args.warmup, flush)
+    f = plan.flat
+    nidx = int((f["ncart"] * f["nprim"]).sum())
+    res = {"metric": "AO overlap matrices/s (S, dS/dx, dS/dy, dS/dz per step)", "unit": "matrices/s",
+           "value": 4 / (ms * 1e-3), "ms_per_step": ms, "dtype": "f64",
+           "config": {"workload": "overlap: 200 atoms, %d Cartesian AOs, %d spherical, %d (row, primitive) pairs"
+                      % (plan.ncart, plan.nao, nidx), "api": "analytical_integrals.get_ao_overlap"}}
+    # end to end through the public call (host geometry in, host matrix out)
+    t = time.perf_counter()
+    for d in (None, "x", "y", "z"):
+        ai.get_ao_overlap(geo, geo, qc.ao_spec, drv=d)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t
+    res["e2e"] = {"value": 4 / e2e_s, "unit": "matrices/s", "h2d_bytes_per_step": 2 * geo.nbytes * 4,
+                  "d2h_bytes_per_step": 4 * plan.nao * plan.nao * 8}
+    res["gpu_launches"] = 8
+    if not args.no_cpu_baseline:
+        okref = _oracle()
+        lx = qc.ao_spec.get_lxlylz()
+        t = time.perf_counter()
+        okref.aooverlap(geo, geo, lx, lx, qc.ao_spec, 0)
+        dt = time.perf_counter() - t
+        res["cpu_baseline"] = {"value": 1 / dt, "unit": "matrices/s", "cores": 1, "kind": "port",
+                               "sample": "one raw Cartesian overlap matrix (cy_overlap.aooverlap restated in C), "
+                                         "%.2f s" % dt}
+    return res
+
+
+def _detci_workload(args, flush):
+    """CI transition density and flux density (detci.rho + detci.jab) from MO grids:
+    the determinant-comparison terms of the first state pair of the H3+ FCI test
+    (436 zero terms, 7160 single-excitation terms over 42 MOs) on 2^21 points of
+    seeded MO grids."""
+    import torch
+    from orbkit_gb300 import _lib, detci
+    d = numpy.load(os.path.join(ROOT, "tests", "golden", "h3p_detci.npz"))
+    npts, nmo = 1 << 21, 42
+    zc, zi = d["zero_coef_0"], d["zero_orb_0"]
+    sc, sp = d["sing_coef_0"], d["sing_pair_0"]
+    g = torch.Generator(device="cuda").manual_seed(7)
+    mo = torch.randn((nmo, npts), generator=g, dtype=torch.float64, device="cuda")
+    drv = torch.randn((3, nmo, npts), generator=g, dtype=torch.float64, device="cuda")
+    rho = torch.empty(npts, dtype=torch.float64, device="cuda")
+    j = torch.empty((3, npts), dtype=torch.float64, device="cuda")
+    L = detci._L()
+    keep = [torch.from_numpy(numpy.ascontiguousarray(a)).cuda() for a in (zc, zi.astype(numpy.int32), sc,
+                                                                           sp.astype(numpy.int32))]
+
+    def step():
+        _lib.check(L.okg_ci_rho(npts, _lib.ptr(mo), npts, len(zc), _lib.ptr(keep[0]), _lib.ptr(keep[1]), len(sc),
+                                _lib.ptr(keep[2]), _lib.ptr(keep[3]), _lib.ptr(rho), _lib.stream_handle()))
+        _lib.check(L.okg_ci_jab(npts, _lib.ptr(mo), _lib.ptr(drv), npts, nmo, len(sc), _lib.ptr(keep[2]),
+                                _lib.ptr(keep[3]), _lib.ptr(j), _lib.stream_handle()))
+    ms = _time_ms(step, args.steps, args.warmup, flush)
+    res = {"metric": "grid points/s for the CI transition density + flux density from MO grids",
+           "unit": "grid points/s", "value": npts / (ms * 1e-3), "ms_per_step": ms, "dtype": "f64",
+           "config": {"workload": "detci: %d zero + %d single terms over %d MOs, %d points (rho then jab)"
+                      % (len(zc), len(sc), nmo, npts),
+                      "terms_per_point": len(zc) + 4 * len(sc), "api": "okg_ci_rho + okg_ci_jab",
+                      "min_dram_bytes_per_step": 8 * (4 * nmo * npts + 4 * npts)}}
+    res["gpu_launches"] = 2
+    if not args.no_cpu_baseline:
+        okref = _oracle()
+        zero = [[list(zc)], [list(int(v) for v in zi)]]
+        sing = [list(sc), [list(map(int, p)) for p in sp]]
+        n = 4096
+        m = mo[:, :n].cpu().numpy()
+        md = drv[:, :, :n].cpu().numpy()
+        t = time.perf_counter()
+        okref.ci_rho(zero, sing, m)
+        okref.ci_jab(zero, sing, m, md)
+        dt = time.perf_counter() - t
+        res["cpu_baseline"] = {"value": n / dt, "unit": "grid points/s", "cores": 1, "kind": "port",
+                               "sample": "%d points, the same terms (numpy restatement of cy_ci), %.2f s" % (n, dt)}
+    return res
 
 
 def ctypes_fp64_rate(L):
@@ -534,7 +639,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--profile", action="store_true", help="minimal launch sequence for ncu captures")
-    ap.add_argument("--workload", default="mid", choices=["mid", "small", "grad", "batch", "large"])
+    ap.add_argument("--workload", default="mid", choices=["mid", "small", "grad", "batch", "large", "overlap", "detci"])
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)

@@ -228,6 +228,32 @@ int okg_ci_jab(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld
 int okg_ci_a_nabla_b(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld, int nmo, int ns,
                      const double* d_scoef, const int* d_spair, double* d_j, okg_stream stream);
 
+/* ------------------------------------------------------------ AO overlap
+ * Analytic overlap of contracted Cartesian Gaussians, FP64:
+ * replaces cy_overlap.aooverlap (orbkit/cy_overlap.pyx:78-163, with get_overlap of
+ * orbkit/c_non-grid-based.c:9-52) and the 'N' factor / cartesian2spherical_aoom steps
+ * of get_ao_overlap (orbkit/analytical_integrals.py:37-182).
+ * The plan takes the arrays of okg_basis_create plus the primitives (h_prim,
+ * nprim x 2 [alpha, c]; ao_spec.get_prim_coeffs()) on the host; per (listed row,
+ * primitive) norms ao_norm (orbkit/c_support.c:177-188) are computed once from the
+ * bra exponents h_lxlylz, as orbkit does for both bra and ket. */
+typedef struct okg_overlap_plan okg_overlap_plan;
+int okg_overlap_plan_create(int natom, int nshell, const int* h_shell_atom, const int* h_shell_ncart,
+                            const int* h_shell_nprim, const int* h_lxlylz, int is_normalized, const double* h_prim,
+                            const double* h_renorm, int nsph, const int* h_sph_ptr, const int* h_sph_cart,
+                            const double* h_sph_coef, okg_overlap_plan** out);
+int okg_overlap_plan_destroy(okg_overlap_plan* plan);
+/* Listed Cartesian rows and output rows (spherical if the plan has a transform). */
+int okg_overlap_plan_info(const okg_overlap_plan* plan, int* ncart, int* nao);
+/* Ket exponents (ncart x 3; get_ao_overlap's lxlylz_b), NULL = the bra's.  Synchronous. */
+int okg_overlap_plan_set_ket(okg_overlap_plan* plan, const int* h_lxlylz_b);
+/* d_out[I * ld + J] = <bra I at d_geo_a | d^drv ket J at d_geo_b> (natom x 3 each, on the
+ * device); drv 0 none, 1..3 d/dx, d/dy, d/dz of the ket.  raw = 1 returns the Cartesian
+ * matrix of cy_overlap.aooverlap; raw = 0 applies the 'N' factor and the spherical
+ * transform as get_ao_overlap does (nao x nao). */
+int okg_ao_overlap(okg_overlap_plan* plan, const double* d_geo_a, const double* d_geo_b, int drv, int raw,
+                   double* d_out, int64_t ld, okg_stream stream);
+
 /* Diagnostic (no counterpart in orbkit): measured FP64 FMA rate of the current device
  * in FMA/s, from a kernel of independent FMA chains (synchronising; allocates). */
 int okg_diag_fp64_fma_rate(long long iters, double* fma_per_s);

@@ -19,6 +19,9 @@
  *   okref_rho_threads            the same per slice, slices spread over POSIX threads
  *                                (the reference spreads them over processes,
  *                                core.py:524-537)
+ *   okref_aooverlap              orbkit/cy_overlap.pyx:78-163 with get_overlap / s of
+ *                                orbkit/c_non-grid-based.c:9-52 (analytic AO overlap)
+ *   okref_mooverlapmatrix        orbkit/cy_overlap.pyx:184-205
  */
 #include <math.h>
 #include <pthread.h>
@@ -325,4 +328,99 @@ int okref_rho_threads(const okref_basis* b, const double* x, const double* y, co
     free(th);
     pthread_mutex_destroy(&J.lock);
     return J.err;
+}
+
+/* ------------------------------------------------------------------ AO overlap
+ * 1D overlap factor s(a, b) along axis i of primitives at RA (exponent al) and
+ * RB (exponent be): the recursion orbkit uses (orbkit/c_non-grid-based.c:33-52,
+ * after M. Ho and J. M. Hernandez-Perez, Mathematica Journal 14 (2012)). */
+static double ov_s(int i, int a, int b, const double* RA, const double* RB, double al, double be)
+{
+    if (b > 0) return ov_s(i, a + 1, b - 1, RA, RB, al, be) + (RA[i] - RB[i]) * ov_s(i, a, b - 1, RA, RB, al, be);
+    if (a == 0) return 1.;
+    const double xpa = -(RA[i] - (al * RA[i] + be * RB[i]) / (al + be));
+    if (a == 1) return xpa;
+    return xpa * ov_s(i, a - 1, 0, RA, RB, al, be) + ((a - 1) / (2. * (al + be))) * ov_s(i, a - 2, 0, RA, RB, al, be);
+}
+
+/* Primitive overlap (orbkit/c_non-grid-based.c:9-31). */
+static double ov_prim(const double* RA, const int* la, double al, const double* RB, const int* lb, double be)
+{
+    double rr = 0;
+    for (int i = 0; i < 3; i++) rr += (RA[i] - RB[i]) * (RA[i] - RB[i]);
+    double ov = exp(-((al * be) / (al + be)) * rr) * pow(M_PI / (al + be), 3. / 2.);
+    for (int i = 0; i < 3; i++) ov *= ov_s(i, la[i], lb[i], RA, RB, al, be);
+    return ov;
+}
+
+/* cy_overlap.aooverlap (orbkit/cy_overlap.pyx:78-163): aoom (ncart x ncart, zeroed
+ * by the caller) over the flattened (shell, row, primitive) list, bra outer, ket
+ * inner; drv 1..3 differentiates the ket along x, y, z. */
+void okref_aooverlap(double* aoom, const double* geo_a, const double* geo_b, const int* lxlylz_a,
+                     const int* lxlylz_b, const int* assign, const double* coeffs, const int* pnum, const int* atoms,
+                     int nshell, int drv, int is_normalized)
+{
+    int nidx = 0, ncart = 0;
+    for (int s = 0; s < nshell; s++) {
+        nidx += assign[s] * pnum[s];
+        ncart += assign[s];
+    }
+    int* row = (int*)malloc(sizeof(int) * (size_t)nidx);
+    int* prm = (int*)malloc(sizeof(int) * (size_t)nidx);
+    int* atm = (int*)malloc(sizeof(int) * (size_t)nidx);
+    double* nrm = (double*)malloc(sizeof(double) * (size_t)nidx);
+    int c = 0, c_ao = 0, c_p = 0;
+    for (int s = 0; s < nshell; s++) {
+        for (int r = 0; r < assign[s]; r++)
+            for (int q = 0; q < pnum[s]; q++) {
+                const int* l = lxlylz_a + 3 * (c_ao + r);
+                nrm[c] = okref_ao_norm(l[0], l[1], l[2], coeffs[2 * (c_p + q)], is_normalized);
+                row[c] = c_ao + r;
+                prm[c] = c_p + q;
+                atm[c] = atoms[s];
+                c++;
+            }
+        c_ao += assign[s];
+        c_p += pnum[s];
+    }
+    for (int i = 0; i < nidx; i++)
+        for (int j = 0; j < nidx; j++) {
+            const double* RA = geo_a + 3 * atm[i];
+            const double* RB = geo_b + 3 * atm[j];
+            const int* la = lxlylz_a + 3 * row[i];
+            int lb[3] = {lxlylz_b[3 * row[j]], lxlylz_b[3 * row[j] + 1], lxlylz_b[3 * row[j] + 2]};
+            const double al = coeffs[2 * prm[i]], be = coeffs[2 * prm[j]];
+            const double ci = coeffs[2 * prm[i] + 1], cj = coeffs[2 * prm[j] + 1];
+            double* out = aoom + (long)row[i] * ncart + row[j];
+            if (drv <= 0) {
+                *out += ci * cj * nrm[i] * nrm[j] * ov_prim(RA, la, al, RB, lb, be);
+                continue;
+            }
+            const int d = drv - 1, l0 = lb[d];
+            if (l0 > 0) {
+                lb[d] = l0 - 1;
+                *out += l0 * ci * cj * nrm[i] * nrm[j] * ov_prim(RA, la, al, RB, lb, be);
+            }
+            lb[d] = l0 + 1;
+            *out += (-2 * be) * ci * cj * nrm[i] * nrm[j] * ov_prim(RA, la, al, RB, lb, be);
+        }
+    free(row);
+    free(prm);
+    free(atm);
+    free(nrm);
+    (void)ncart;
+}
+
+/* cy_overlap.mooverlapmatrix (orbkit/cy_overlap.pyx:184-205): moom[i,j] =
+ * sum_k sum_l a[i,k] b[j,l] S[k,l], k outer, l inner. */
+void okref_mooverlapmatrix(double* moom, const double* A, const double* B, const double* S, int nmo_a, int nmo_b,
+                           int nao, int mao)
+{
+    for (int i = 0; i < nmo_a; i++)
+        for (int j = 0; j < nmo_b; j++) {
+            double t = 0.0;
+            for (int k = 0; k < nao; k++)
+                for (int l = 0; l < mao; l++) t += A[(long)i * nao + k] * B[(long)j * mao + l] * S[(long)k * mao + l];
+            moom[(long)i * nmo_b + j] = t;
+        }
 }

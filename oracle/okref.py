@@ -61,6 +61,8 @@ def lib():
         L.okref_ao_norm.restype = ctypes.c_double
         L.okref_slice_rho.restype = ctypes.c_int
         L.okref_rho_threads.restype = ctypes.c_int
+        L.okref_aooverlap.argtypes = [dp, dp, dp, ip, ip, ip, dp, ip, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.okref_mooverlapmatrix.argtypes = [dp, dp, dp, dp] + [ctypes.c_int] * 4
         _lib = L
     return _lib
 
@@ -511,3 +513,115 @@ def ci_driver(fn, zero, sing, molist, *rest, slice_length=1e4):
     n = flat.shape[-1]
     flat[..., ci_covered(n, slice_length):] = 0.0
     return flat.reshape(shape)
+
+
+# ------------------------------------------------------------------ AO overlap
+def aooverlap(coord_a, coord_b, lxlylz_a, lxlylz_b, ao_spec, drv):
+    """cy_overlap.aooverlap (orbkit/cy_overlap.pyx:78-163) -> (NAOcart, NAOcart)."""
+    lxa = _i(lxlylz_a)
+    lxb = _i(lxlylz_b)
+    assign = _i(ao_spec.get_nlxlylz_per_cont())
+    coeffs = _f(ao_spec.get_prim_coeffs())
+    pnum = _i(ao_spec.get_nprim_per_cont())
+    atoms = _i(ao_spec.get_assign_cont_to_atoms())
+    out = numpy.zeros((len(lxa), len(lxa)))
+    lib().okref_aooverlap(_p(out), _p(_f(coord_a)), _p(_f(coord_b)), _p(lxa, ctypes.c_int), _p(lxb, ctypes.c_int),
+                          _p(assign, ctypes.c_int), _p(coeffs), _p(pnum, ctypes.c_int), _p(atoms, ctypes.c_int),
+                          len(assign), int(drv), int(ao_spec.get_normalized()))
+    return out
+
+
+def cartesian2spherical_aoom(aoom, ao_spec):
+    """orbkit/analytical_integrals.py:118-182, evaluated in the same order: for every
+    output pair (i0, i1) the terms are added component of i0 outer, of i1 inner, each
+    (coef0 fac0 coef1 fac1) S[row0, row1]."""
+    tab = _cart2sph_lookup()
+    lxlylz = ao_spec.get_lxlylz()
+    assign = ao_spec.get_assign_lxlylz_to_cont()
+    sph = ao_spec.get_old_ao_spherical()
+    rows = [[] for _ in range(len(ao_spec))]
+    for i, j in enumerate(assign):
+        rows[j].append(i)
+    terms = []  # per spherical row: list of (coef, fac, Cartesian row)
+    for (j0, k0) in sph:
+        comps, coefs, fac = tab(*k0)
+        t = []
+        for c0, comp in enumerate(comps):
+            for i, j in enumerate(rows[j0]):
+                if tuple(lxlylz[j]) == comp:
+                    t.append((coefs[c0], fac, i + rows[j0][0]))
+        terms.append(t)
+    n = len(sph)
+    out = numpy.zeros((n, n))
+    for i0 in range(n):
+        for (a0, f0, r0) in terms[i0]:
+            for i1 in range(n):
+                for (a1, f1, r1) in terms[i1]:
+                    out[i0, i1] += a0 * f0 * a1 * f1 * aoom[r0, r1]
+    return out
+
+
+def ao_overlap(coord_a, coord_b, ao_spec, lxlylz_b=None, drv=None):
+    """get_ao_overlap (orbkit/analytical_integrals.py:37-116): aooverlap, then the
+    'N' factor on rows and columns, then the spherical transform."""
+    if isinstance(drv, list) or (isinstance(drv, str) and len(drv) > 1):
+        return [ao_overlap(coord_a, coord_b, ao_spec, lxlylz_b=lxlylz_b, drv=d) for d in drv]
+    lxa = ao_spec.get_lxlylz()
+    lxb = numpy.array(lxa, copy=True) if lxlylz_b is None else numpy.array(lxlylz_b, dtype=numpy.intc)
+    drv = validate_drv(drv)
+    if drv > 3:
+        raise ValueError("Only first derivatives are supported for analytical integrals.")
+    S = aooverlap(coord_a, coord_b, lxa, lxb, ao_spec, drv)
+    if "N" in ao_spec[0]:
+        N = numpy.asarray(ao_spec[0]["N"], dtype=numpy.float64)
+        for i in range(len(S)):
+            S[i, :] *= N[i] * N[:, 0]
+    if getattr(ao_spec, "spherical", False):
+        S = cartesian2spherical_aoom(S, ao_spec)
+    return S
+
+
+def mo_overlap_matrix(mo_a, mo_b, aoom):
+    """cy_overlap.mooverlapmatrix over all rows (orbkit/cy_overlap.pyx:184-205)."""
+    A, B, S = _f(mo_a), _f(mo_b), _f(aoom)
+    out = numpy.zeros((A.shape[0], B.shape[0]))
+    lib().okref_mooverlapmatrix(_p(out), _p(A), _p(B), _p(S), A.shape[0], B.shape[0], S.shape[0], S.shape[1])
+    return out
+
+
+def ao_dipole_matrix(qc, component):
+    """get_ao_dipole_matrix (orbkit/analytical_integrals.py:363-414): overlap with the
+    ket exponent along `component` raised by one, plus the overlap with column i
+    scaled by the coordinate of AO i's atom."""
+    c = "xyz".find(component) if isinstance(component, str) else int(component)
+    lxb = numpy.array(qc.ao_spec.get_lxlylz(), dtype=numpy.intc)
+    lxb[:, c] += 1
+    part1 = ao_overlap(qc.geo_spec, qc.geo_spec, qc.ao_spec, lxlylz_b=lxb)
+    part2 = ao_overlap(qc.geo_spec, qc.geo_spec, qc.ao_spec)
+    sph = getattr(qc.ao_spec, "spherical", False)
+    per = (numpy.bincount(qc.ao_spec.get_assign_lm_to_cont(), minlength=len(qc.ao_spec)) if sph
+           else qc.ao_spec.get_nlxlylz_per_cont())
+    i = 0
+    for s, n in zip(qc.ao_spec, per):
+        for _ in range(n):
+            part2[:, i] *= qc.geo_spec[s["atom"], c]
+            i += 1
+    return part1 + part2
+
+
+def dipole_moment(qc, charges, component=("x", "y", "z")):
+    """get_dipole_moment (orbkit/analytical_integrals.py:328-361) with the nuclear
+    charges given explicitly (orbkit reads them from geo_info[:, 2])."""
+    coeffs = qc.mo_spec.get_coeffs()
+    occ = qc.mo_spec.get_occ()
+    out = numpy.zeros(len(component))
+    for k, c in enumerate(component):
+        D = ao_dipole_matrix(qc, c)
+        for i in range(len(coeffs)):
+            out[k] -= occ[i] * mo_overlap_matrix(coeffs[i:i + 1], coeffs[i:i + 1], D)[0, 0]
+        ci = "xyz".find(c)
+        nuc = 0.0
+        for a in range(len(qc.geo_spec)):
+            nuc += float(charges[a]) * qc.geo_spec[a][ci]
+        out[k] += nuc
+    return out

@@ -4,7 +4,7 @@ import numpy
 import pytest
 
 import okref
-from helpers import is_x86, load_golden
+from helpers import GOLDEN, is_x86, load_golden
 
 DRV_ALL = [None, "x", "y", "z", "xx", "yy", "zz", "xy", "xz", "yz"]
 
@@ -170,3 +170,30 @@ def test_detci_golden():
         for name, a, b in (("rho", r, d["rho_01"][k]), ("j", j, d["j_01"][k]), ("nabla j", nj, d["nabla_j_01"][k])):
             assert numpy.abs(a - b).max() <= 1e-14 * numpy.abs(b).max(), (k, name, numpy.abs(a - b).max())
         assert d["rho_01"][k].reshape(-1)[-1] == 0.0 and okref.ci_rho(zero, sing, mo[0]).reshape(-1)[-1] != 0.0
+
+
+OVERLAP_FIXTURES = ("h2o_molden", "small_cart", "sph_fg_N", "normalized")
+
+
+@pytest.mark.parametrize("name", OVERLAP_FIXTURES)
+def test_overlap_golden(name):
+    """Analytic AO overlap, its ket derivatives, a second ket geometry, a ket exponent
+    override, dipole matrices, MO overlap matrices and the dipole moment: the oracle
+    against the reference's outputs (tests/golden/overlap.npz)."""
+    qc, _ = load_golden(name + ".npz")
+    g = numpy.load(GOLDEN + "/overlap.npz")
+    G = {k.split("__", 1)[1]: g[k] for k in g.files if k.startswith(name + "__")}
+    geo = qc.geo_spec
+    S = okref.ao_overlap(geo, geo, qc.ao_spec)
+    _same(S, G["S"], "S")
+    _same(numpy.array(okref.ao_overlap(geo, geo, qc.ao_spec, drv=["x", "y", "z"])), G["Sd"], "dS")
+    S2 = okref.ao_overlap(geo, G["geo2"], qc.ao_spec)
+    _same(S2, G["S2"], "S(geo, geo2)")
+    _same(numpy.array(okref.ao_overlap(geo, G["geo2"], qc.ao_spec, drv=["x", "y", "z"])), G["S2d"], "dS(geo, geo2)")
+    _same(okref.ao_overlap(geo, geo, qc.ao_spec, lxlylz_b=G["lxlylz_ket"]), G["Sket"], "S ket exponents")
+    mo = qc.mo_spec.get_coeffs()
+    _same(okref.mo_overlap_matrix(mo, mo, S), G["moom"], "MO overlap")
+    _same(okref.mo_overlap_matrix(mo, mo, S2), G["moom2"], "MO overlap (geo, geo2)")
+    D = numpy.array([okref.ao_dipole_matrix(qc, c) for c in "xyz"])
+    _same(D, G["dip"], "dipole matrices")
+    _same(okref.dipole_moment(qc, G["charges"]), G["dipole"], "dipole moment")
