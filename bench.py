@@ -577,13 +577,17 @@ def _detci_workload(args, flush):
     """CI transition density and flux density (detci.rho + detci.jab) from MO grids:
     the determinant-comparison terms of the first state pair of the H3+ FCI test
     (436 zero terms, 7160 single-excitation terms over 42 MOs) on 2^21 points of
-    seeded MO grids."""
+    seeded MO grids.  value: the default evaluation (terms folded into 42 x 42
+    matrices, okg_ci_rho_matrix + okg_ci_flux_matrix); term_order: orbkit's term-order
+    sums (okg_ci_rho + okg_ci_jab)."""
     import torch
     from orbkit_gb300 import _lib, detci
     d = numpy.load(os.path.join(ROOT, "tests", "golden", "h3p_detci.npz"))
     npts, nmo = 1 << 21, 42
     zc, zi = d["zero_coef_0"], d["zero_orb_0"]
     sc, sp = d["sing_coef_0"], d["sing_pair_0"]
+    zero = [[list(zc)], [list(int(v) for v in zi)]]
+    sing = [list(sc), [list(map(int, p)) for p in sp]]
     g = torch.Generator(device="cuda").manual_seed(7)
     mo = torch.randn((nmo, npts), generator=g, dtype=torch.float64, device="cuda")
     drv = torch.randn((3, nmo, npts), generator=g, dtype=torch.float64, device="cuda")
@@ -592,24 +596,50 @@ def _detci_workload(args, flush):
     L = detci._L()
     keep = [torch.from_numpy(numpy.ascontiguousarray(a)).cuda() for a in (zc, zi.astype(numpy.int32), sc,
                                                                            sp.astype(numpy.int32))]
+    M = detci.density_matrix(zero, sing, nmo)
+    S = M + M.T
+    S[numpy.diag_indices(nmo)] = numpy.diag(M)
+    q_rho = detci._qt_device(numpy.tril(S), nmo)
+    C = detci.flux_matrix(sing, nmo)
+    q_jab = detci._qt_device((C - C.T).T, nmo)
+    st = _lib.stream_handle()
 
-    def step():
+    def step_terms():
         _lib.check(L.okg_ci_rho(npts, _lib.ptr(mo), npts, len(zc), _lib.ptr(keep[0]), _lib.ptr(keep[1]), len(sc),
-                                _lib.ptr(keep[2]), _lib.ptr(keep[3]), _lib.ptr(rho), _lib.stream_handle()))
+                                _lib.ptr(keep[2]), _lib.ptr(keep[3]), _lib.ptr(rho), st))
         _lib.check(L.okg_ci_jab(npts, _lib.ptr(mo), _lib.ptr(drv), npts, nmo, len(sc), _lib.ptr(keep[2]),
-                                _lib.ptr(keep[3]), _lib.ptr(j), _lib.stream_handle()))
-    ms = _time_ms(step, args.steps, args.warmup, flush)
+                                _lib.ptr(keep[3]), _lib.ptr(j), st))
+
+    def step_matrix():
+        _lib.check(L.okg_ci_rho_matrix(npts, _lib.ptr(mo), npts, nmo, _lib.ptr(q_rho), _lib.ptr(rho), st))
+        _lib.check(L.okg_ci_flux_matrix(npts, _lib.ptr(mo), _lib.ptr(drv), npts, nmo, _lib.ptr(q_jab), -0.5,
+                                        _lib.ptr(j), st))
+    ms = _time_ms(step_matrix, args.steps, args.warmup, flush)
+    r_m, j_m = rho.clone(), j.clone()
+    ms_terms = _time_ms(step_terms, max(2, args.steps // 2), 1, flush)
+    err = max(float((r_m - rho).abs().max() / rho.abs().max()), float((j_m - j).abs().max() / j.abs().max()))
+    # FMAs the quadratic forms issue per point: rho visits a <= b in chunks of 16, the
+    # flux all (a, b) plus three accumulations per b
+    ch = (nmo + 15) // 16
+    fma_rho = sum(16 * (nmo - 16 * c) for c in range(ch)) + sum(nmo - 16 * c for c in range(ch))
+    fma_jab = ch * nmo * (16 + 3)
+    fma_rate = (fma_rho + fma_jab) * npts / (ms * 1e-3)
+    peak = ctypes_fp64_rate(_lib.load())
     res = {"metric": "grid points/s for the CI transition density + flux density from MO grids",
            "unit": "grid points/s", "value": npts / (ms * 1e-3), "ms_per_step": ms, "dtype": "f64",
            "config": {"workload": "detci: %d zero + %d single terms over %d MOs, %d points (rho then jab)"
                       % (len(zc), len(sc), nmo, npts),
-                      "terms_per_point": len(zc) + 4 * len(sc), "api": "okg_ci_rho + okg_ci_jab",
-                      "min_dram_bytes_per_step": 8 * (4 * nmo * npts + 4 * npts)}}
-    res["gpu_launches"] = 2
+                      "api": "okg_ci_rho_matrix + okg_ci_flux_matrix (detci.rho / detci.jab default)",
+                      "term_order": {"value": npts / (ms_terms * 1e-3), "ms_per_step": ms_terms,
+                                     "api": "okg_ci_rho + okg_ci_jab (exact=True)"},
+                      "max_normwise_diff_vs_term_order": err},
+           "roofline": {"bound": "fp64", "achieved": fma_rate, "peak": peak, "unit": "FMA/s",
+                        "frac": (fma_rate / peak) if peak else None, "traffic": None,
+                        "note": "FMAs issued per point %d (rho) + %d (flux); peak = okg_diag_fp64_fma_rate"
+                                % (fma_rho, fma_jab)},
+           "gpu_launches": 2}
     if not args.no_cpu_baseline:
         okref = _oracle()
-        zero = [[list(zc)], [list(int(v) for v in zi)]]
-        sing = [list(sc), [list(map(int, p)) for p in sp]]
         n = 4096
         m = mo[:, :n].cpu().numpy()
         md = drv[:, :, :n].cpu().numpy()
@@ -625,7 +655,7 @@ def _detci_workload(args, flush):
 def ctypes_fp64_rate(L):
     import ctypes
     v = ctypes.c_double(0)
-    if L.okg_diag_fp64_fma_rate(4000, ctypes.byref(v)) != 0:
+    if L.okg_diag_fp64_fma_rate(20000, ctypes.byref(v)) != 0:
         return None
     return v.value
 

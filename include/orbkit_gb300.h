@@ -228,6 +228,21 @@ int okg_ci_jab(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld
 int okg_ci_a_nabla_b(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld, int nmo, int ns,
                      const double* d_scoef, const int* d_spair, double* d_j, okg_stream stream);
 
+/* The same sums as quadratic forms (no counterpart in orbkit; a faster evaluation
+ * of ci_core.rho / jab / a_nabla_b, orbkit/detci/ci_core.py:84-267): the host folds
+ * the terms into NMO x NMO matrices and a point costs NMO^2 FMAs whatever the
+ * number of terms.  d_qt holds nmo rows of ldq = nmo rounded up to a multiple of 16
+ * doubles (zero padded, 16-byte aligned).
+ * rho[p] = sum_b MO_b(p) sum_{a <= b} qt[b*ldq + a] MO_a(p)   (qt lower triangular:
+ *          the symmetrised density matrix, M_ab + M_ba off the diagonal) */
+int okg_ci_rho_matrix(int64_t npts, const double* d_mo, int64_t ld, int nmo, const double* d_qt, double* d_rho,
+                      okg_stream stream);
+/* j[d*npts + p] = scale sum_b dMO_b(p) sum_a qt[b*ldq + a] MO_a(p), d = x, y, z
+ * (jab: qt = C^T - C, scale = -1/2; a_nabla_b: qt = C^T, scale = 1, with C_ab the
+ * summed coefficients of the single-excitation terms (a, b)). */
+int okg_ci_flux_matrix(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld, int nmo,
+                       const double* d_qt, double scale, double* d_j, okg_stream stream);
+
 /* ------------------------------------------------------------ AO overlap
  * Analytic overlap of contracted Cartesian Gaussians, FP64:
  * replaces cy_overlap.aooverlap (orbkit/cy_overlap.pyx:78-163, with get_overlap of

@@ -65,6 +65,60 @@ __global__ void ci_flux_kernel(long long npts, const double* __restrict__ mo, co
     for (int d = 0; d < 3; ++d) j[(long long)d * npts + p] = acc[d];
 }
 
+// Quadratic-form evaluation of the same sums.  The terms collapse into NMO x NMO
+// coefficient matrices (host side): rho = sum_ab M_ab MO_a MO_b and
+// j_d = scale sum_ab Q_ab MO_a dMO_b, so a point costs NMO^2 FMAs instead of work
+// proportional to the number of terms.  Each thread owns one point and walks the
+// bra orbitals in chunks of CI_CH held in registers; per ket orbital b it forms
+// t_b = sum_{a in chunk} Q^T[b][a] MO_a (coefficients read as broadcasts through
+// L1) and adds t_b MO_b (rho) or t_b dMO_b for the three directions (flux), so the
+// flux shares one matrix-vector product between x, y and z.  For rho the matrix is
+// symmetrised and only a <= b is visited (lower triangle of Q^T, zero above).
+// FP64 FMAs; the sum order differs from orbkit's term order.
+#define CI_CH 16
+
+template <bool FLUX>
+__global__ void __launch_bounds__(128) ci_quad_kernel(long long npts, const double* __restrict__ mo,
+                                                      const double* __restrict__ drv, long long ld, int nmo,
+                                                      const double* __restrict__ qt, double scale,
+                                                      double* __restrict__ out)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    const long long dstride = (long long)nmo * ld;
+    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+    for (int a0 = 0; a0 < nmo; a0 += CI_CH) {
+        double pa[CI_CH];
+#pragma unroll
+        for (int i = 0; i < CI_CH; ++i) pa[i] = (a0 + i < nmo) ? mo[(long long)(a0 + i) * ld + p] : 0.0;
+        // rho: rows b < a0 of the lower-triangular Q^T hold zeros for this chunk
+        for (int b = FLUX ? 0 : a0; b < nmo; ++b) {
+            const double2* q = reinterpret_cast<const double2*>(qt + (long long)b * ((nmo + CI_CH - 1) / CI_CH * CI_CH) + a0);
+            double t = 0.0;
+#pragma unroll
+            for (int i = 0; i < CI_CH / 2; ++i) {
+                const double2 c = __ldg(q + i);
+                t = fma(c.x, pa[2 * i], t);
+                t = fma(c.y, pa[2 * i + 1], t);
+            }
+            if (FLUX) {
+                acc0 = fma(t, drv[(long long)b * ld + p], acc0);
+                acc1 = fma(t, drv[dstride + (long long)b * ld + p], acc1);
+                acc2 = fma(t, drv[2 * dstride + (long long)b * ld + p], acc2);
+            } else {
+                acc0 = fma(t, mo[(long long)b * ld + p], acc0);
+            }
+        }
+    }
+    if (FLUX) {
+        out[p] = scale * acc0;
+        out[npts + p] = scale * acc1;
+        out[2 * npts + p] = scale * acc2;
+    } else {
+        out[p] = scale * acc0;
+    }
+}
+
 }  // namespace okg
 
 using namespace okg;
@@ -119,4 +173,30 @@ extern "C" int okg_ci_a_nabla_b(int64_t npts, const double* d_mo, const double* 
 {
     return ci_flux(false, npts, d_mo, d_drv, ld, nmo, ns, d_scoef, d_spair, d_j, (cudaStream_t)stream,
                    "okg_ci_a_nabla_b: bad argument (NULL pointer, npts < 0, ld < npts, nmo <= 0 or ns < 0)");
+}
+
+// Q^T is nmo rows of ldq = nmo rounded up to a multiple of 16 doubles (zero padded;
+// 16-byte aligned rows).
+extern "C" int okg_ci_rho_matrix(int64_t npts, const double* d_mo, int64_t ld, int nmo, const double* d_qt,
+                                 double* d_rho, okg_stream stream)
+{
+    if (npts < 0 || !d_rho || (npts > 0 && (!d_mo || !d_qt)) || ld < npts || nmo <= 0)
+        return set_error(OKG_ERR_ARG, "okg_ci_rho_matrix: bad argument (NULL pointer, npts < 0, ld < npts, nmo <= 0)");
+    if (((uintptr_t)d_qt & 15) != 0) return set_error(OKG_ERR_ARG, "okg_ci_rho_matrix: d_qt not 16-byte aligned");
+    if (npts == 0) return OKG_OK;
+    const unsigned nblk = (unsigned)((npts + 127) / 128);
+    ci_quad_kernel<false><<<nblk, 128, 0, (cudaStream_t)stream>>>(npts, d_mo, nullptr, ld, nmo, d_qt, 1.0, d_rho);
+    return cuda_status(cudaGetLastError(), "okg_ci_rho_matrix launch");
+}
+
+extern "C" int okg_ci_flux_matrix(int64_t npts, const double* d_mo, const double* d_drv, int64_t ld, int nmo,
+                                  const double* d_qt, double scale, double* d_j, okg_stream stream)
+{
+    if (npts < 0 || !d_j || (npts > 0 && (!d_mo || !d_drv || !d_qt)) || ld < npts || nmo <= 0)
+        return set_error(OKG_ERR_ARG, "okg_ci_flux_matrix: bad argument (NULL pointer, npts < 0, ld < npts, nmo <= 0)");
+    if (((uintptr_t)d_qt & 15) != 0) return set_error(OKG_ERR_ARG, "okg_ci_flux_matrix: d_qt not 16-byte aligned");
+    if (npts == 0) return OKG_OK;
+    const unsigned nblk = (unsigned)((npts + 127) / 128);
+    ci_quad_kernel<true><<<nblk, 128, 0, (cudaStream_t)stream>>>(npts, d_mo, d_drv, ld, nmo, d_qt, scale, d_j);
+    return cuda_status(cudaGetLastError(), "okg_ci_flux_matrix launch");
 }

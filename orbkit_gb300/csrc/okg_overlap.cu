@@ -6,9 +6,12 @@
 //
 // One thread per output Cartesian pair (I, J).  It walks the primitives of I (outer)
 // and of J (inner), which is the order orbkit's flattened primitive loop adds them
-// to aoom[I, J], and evaluates every product and sum as orbkit writes it (no FMA
-// contraction), so results differ from orbkit's only where the device's exp and pow
-// round differently from the host's.  The 1D factors follow the recursion of
+// to aoom[I, J].  The 1D factors are evaluated with orbkit's operations and
+// rounding (IEEE divisions, no FMA contraction): the two terms of a derivative can
+// cancel to a small fraction of their size, and only this keeps such elements
+// within 1e-12 of orbkit's.  The factors common to all terms of a primitive pair,
+// exp(-mu R^2) and (pi/p)^(3/2), use one reciprocal of p and a square root (a few
+// units in the last place from orbkit's exp/pow values).  The 1D factors follow the recursion of
 // M. Ho and J. M. Hernandez-Perez, "Evaluation of Gaussian Molecular Integrals",
 // Mathematica Journal 14 (2012), doi:10.3888/tmj.14-3, that orbkit uses:
 //   s(0,0) = 1,  s(1,0) = P - A,
@@ -84,7 +87,7 @@ __global__ void ao_overlap_kernel(int nrow, const OvRow* __restrict__ rows, cons
         A[d] = geo_a[3 * ri.atom + d];
         B[d] = geo_b[3 * rj.atom + d];
         AB[d] = A[d] - B[d];
-        rr = __dadd_rn(rr, __dmul_rn(AB[d], AB[d]));
+        rr = fma(AB[d], AB[d], rr);
     }
     const int dd = drv - 1;  // derivative axis or -1
     double v[OKG_OV_MAXV];
@@ -96,9 +99,13 @@ __global__ void ao_overlap_kernel(int nrow, const OvRow* __restrict__ rows, cons
             const double2 pb = prim[rj.prim0 + jp];
             const double nb = pnorm[rj.rp0 + jp];
             const double al = pa.x, be = pb.x;
+            const double inv_p = 1.0 / (al + be);
+            const double arg = al * be * inv_p * rr;
+            if (arg > 746.0) continue;  // exp(-arg) is 0 in double: the pair adds exactly 0
+            const double eab = exp(-arg);
+            const double t = M_PI * inv_p;
+            const double pref = eab * t * sqrt(t);
             const double p = al + be;
-            const double eab = exp(__dmul_rn(-(__dmul_rn(al, be) / p), rr));
-            const double pref = __dmul_rn(eab, pow(M_PI / p, 1.5));
             // product of the 1D factors of the non-derivative axes, in axis order;
             // along the derivative axis the two shifted factors are kept apart
             double s_plain = pref, s_minus = pref, s_plus = pref;

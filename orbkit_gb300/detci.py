@@ -15,6 +15,13 @@ slice_length) (orbkit/detci/ci_core.py:120-125), so the trailing npts % s points
 never evaluated and stay 0 -- its own test data (test/detci/refdata_h3+.npz) hold
 that zero at the last grid point.  By default (reference_slicing=True) those points
 are set to 0 as orbkit leaves them; reference_slicing=False returns every point.
+
+Two evaluations: exact=True walks the terms in orbkit's order with orbkit's
+rounding (okg_ci_rho / okg_ci_jab / okg_ci_a_nabla_b: bit-identical to orbkit for
+the same MO grids, work proportional to the number of terms); the default folds
+the terms into NMO x NMO coefficient matrices on the host (summed in term order)
+and evaluates the quadratic forms (okg_ci_rho_matrix / okg_ci_flux_matrix: NMO^2
+FMAs per point whatever the number of terms, FP64, a different summation order).
 """
 import ctypes
 
@@ -30,6 +37,9 @@ _SIGS = {
                                   _vp, _vp]),
     "okg_ci_a_nabla_b": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _vp,
                                         _vp, _vp, _vp]),
+    "okg_ci_rho_matrix": (ctypes.c_int, [ctypes.c_int64, _vp, ctypes.c_int64, ctypes.c_int, _vp, _vp, _vp]),
+    "okg_ci_flux_matrix": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, ctypes.c_int64, ctypes.c_int, _vp,
+                                          ctypes.c_double, _vp, _vp]),
 }
 
 
@@ -89,25 +99,63 @@ def _out(t, shape, was_tensor):
         tuple(t.shape[:-1]) + tuple(shape))
 
 
-def rho(zero, sing, molist, slice_length=1e4, numproc=1, reference_slicing=True):
+def _qt_device(qt_rows, nmo):
+    """(nmo, ldq) zero-padded copy of Q^T on the device, ldq = nmo rounded up to 16."""
+    import torch
+    ldq = (nmo + 15) // 16 * 16
+    q = numpy.zeros((nmo, ldq))
+    q[:, :nmo] = qt_rows
+    return torch.from_numpy(q).to(_dev())
+
+
+def density_matrix(zero, sing, nmo):
+    """M with rho = sum_ab M_ab MO_a MO_b: the zero terms on the diagonal, the single
+    terms at (a, b), each entry summed in term order."""
+    zc, zi = _zero_terms(zero)
+    sc, sp = _sing_terms(sing)
+    _check_indices(zi, sp, nmo)
+    M = numpy.zeros((nmo, nmo))
+    numpy.add.at(M, (zi, zi), zc)
+    numpy.add.at(M, (sp[:, 0], sp[:, 1]), sc)
+    return M
+
+
+def flux_matrix(sing, nmo):
+    """C with C_ab = sum of the coefficients of the single terms (a, b)."""
+    sc, sp = _sing_terms(sing)
+    _check_indices(numpy.zeros(0, dtype=numpy.int32), sp, nmo)
+    C = numpy.zeros((nmo, nmo))
+    numpy.add.at(C, (sp[:, 0], sp[:, 1]), sc)
+    return C
+
+
+def rho(zero, sing, molist, slice_length=1e4, numproc=1, reference_slicing=True, exact=False):
     """Electron (transition) density on the grid (orbkit/detci/ci_core.py:88-134)."""
     import torch
     L = _L()
     mo, shape, was_t = _grid_tensor(molist, 1)
     nmo, npts = mo.shape
-    zc, zi = _zero_terms(zero)
-    sc, sp = _sing_terms(sing)
-    _check_indices(zi, sp, nmo)
     out = torch.empty((npts,), dtype=torch.float64, device=mo.device)
-    keep = [_to_dev(a) for a in (zc, zi, sc, sp)]
-    _lib.check(L.okg_ci_rho(npts, _lib.ptr(mo), npts, len(zc), _lib.ptr(keep[0]), _lib.ptr(keep[1]), len(sc),
-                            _lib.ptr(keep[2]), _lib.ptr(keep[3]), _lib.ptr(out), _lib.stream_handle()))
+    if exact:
+        zc, zi = _zero_terms(zero)
+        sc, sp = _sing_terms(sing)
+        _check_indices(zi, sp, nmo)
+        keep = [_to_dev(a) for a in (zc, zi, sc, sp)]
+        _lib.check(L.okg_ci_rho(npts, _lib.ptr(mo), npts, len(zc), _lib.ptr(keep[0]), _lib.ptr(keep[1]), len(sc),
+                                _lib.ptr(keep[2]), _lib.ptr(keep[3]), _lib.ptr(out), _lib.stream_handle()))
+    else:
+        M = density_matrix(zero, sing, nmo)
+        S = M + M.T
+        S[numpy.diag_indices(nmo)] = numpy.diag(M)
+        qt = _qt_device(numpy.tril(S), nmo)
+        _lib.check(L.okg_ci_rho_matrix(npts, _lib.ptr(mo), npts, nmo, _lib.ptr(qt), _lib.ptr(out),
+                                       _lib.stream_handle()))
     if reference_slicing:
         out[_covered(npts, slice_length):] = 0.0
     return _out(out, shape, was_t)
 
 
-def _flux(name, zero, sing, molist, molistdrv, slice_length, reference_slicing):
+def _flux(name, zero, sing, molist, molistdrv, slice_length, reference_slicing, exact):
     import torch
     L = _L()
     mo, shape, was_t = _grid_tensor(molist, 1)
@@ -115,27 +163,35 @@ def _flux(name, zero, sing, molist, molistdrv, slice_length, reference_slicing):
     nmo, npts = mo.shape
     if tuple(drv.shape) != (3, nmo, npts):
         raise ValueError("molistdrv must have shape (3,) + molist.shape")
-    sc, sp = _sing_terms(sing)
-    _check_indices(numpy.zeros(0, dtype=numpy.int32), sp, nmo)
     out = torch.empty((3, npts), dtype=torch.float64, device=mo.device)
-    keep = [_to_dev(a) for a in (sc, sp)]
-    _lib.check(getattr(L, name)(npts, _lib.ptr(mo), _lib.ptr(drv), npts, nmo, len(sc), _lib.ptr(keep[0]),
-                                _lib.ptr(keep[1]), _lib.ptr(out), _lib.stream_handle()))
+    if exact:
+        sc, sp = _sing_terms(sing)
+        _check_indices(numpy.zeros(0, dtype=numpy.int32), sp, nmo)
+        keep = [_to_dev(a) for a in (sc, sp)]
+        _lib.check(getattr(L, name)(npts, _lib.ptr(mo), _lib.ptr(drv), npts, nmo, len(sc), _lib.ptr(keep[0]),
+                                    _lib.ptr(keep[1]), _lib.ptr(out), _lib.stream_handle()))
+    else:
+        C = flux_matrix(sing, nmo)
+        # j = scale sum_b dMO_b sum_a Q_ab MO_a: jab Q = C - C^T, scale -1/2; a_nabla_b Q = C
+        Q, scale = (C - C.T, -0.5) if name == "okg_ci_jab" else (C, 1.0)
+        qt = _qt_device(Q.T, nmo)
+        _lib.check(L.okg_ci_flux_matrix(npts, _lib.ptr(mo), _lib.ptr(drv), npts, nmo, _lib.ptr(qt), scale,
+                                        _lib.ptr(out), _lib.stream_handle()))
     if reference_slicing:
         out[:, _covered(npts, slice_length):] = 0.0
     return _out(out, shape, was_t)
 
 
-def jab(zero, sing, molist, molistdrv, slice_length=1e4, numproc=1, reference_slicing=True):
+def jab(zero, sing, molist, molistdrv, slice_length=1e4, numproc=1, reference_slicing=True, exact=False):
     """Imaginary part of the electronic (transition) flux density, (3,) + N
     (orbkit/detci/ci_core.py:143-192)."""
-    return _flux("okg_ci_jab", zero, sing, molist, molistdrv, slice_length, reference_slicing)
+    return _flux("okg_ci_jab", zero, sing, molist, molistdrv, slice_length, reference_slicing, exact)
 
 
-def a_nabla_b(zero, sing, molist, molistdrv, slice_length=1e4, numproc=1, reference_slicing=True):
+def a_nabla_b(zero, sing, molist, molistdrv, slice_length=1e4, numproc=1, reference_slicing=True, exact=False):
     """sum_k c_k MO_a grad MO_b over the single-excitation terms, (3,) + N
     (orbkit/detci/ci_core.py:200-267)."""
-    return _flux("okg_ci_a_nabla_b", zero, sing, molist, molistdrv, slice_length, reference_slicing)
+    return _flux("okg_ci_a_nabla_b", zero, sing, molist, molistdrv, slice_length, reference_slicing, exact)
 
 
 def _check_indices(zi, sp, nmo):

@@ -31,9 +31,9 @@ def test_ci_kernels_bitwise_on_oracle_mos(env):
     for k in range(int(d["npairs"])):
         zero, sing = detci_terms(d, k)
         for sl, rs in ((1e2, True), (1e4, False)):
-            r = detci.rho(zero, sing, mo[0], slice_length=sl, reference_slicing=rs)
-            j = detci.jab(zero, sing, mo[0], mo[1:4], slice_length=sl, reference_slicing=rs)
-            a = detci.a_nabla_b(zero, sing, mo[0], mo[1:4], slice_length=sl, reference_slicing=rs)
+            r = detci.rho(zero, sing, mo[0], slice_length=sl, reference_slicing=rs, exact=True)
+            j = detci.jab(zero, sing, mo[0], mo[1:4], slice_length=sl, reference_slicing=rs, exact=True)
+            a = detci.a_nabla_b(zero, sing, mo[0], mo[1:4], slice_length=sl, reference_slicing=rs, exact=True)
             if rs:
                 r0 = okref.ci_driver(okref.ci_rho, zero, sing, mo[0], slice_length=sl)
                 j0 = okref.ci_driver(okref.ci_jab, zero, sing, mo[0], mo[1:4], slice_length=sl)
@@ -45,6 +45,34 @@ def test_ci_kernels_bitwise_on_oracle_mos(env):
             numpy.testing.assert_array_equal(r, r0)
             numpy.testing.assert_array_equal(j, j0)
             numpy.testing.assert_array_equal(a, a0)
+
+
+def test_ci_quadratic_forms_on_oracle_mos(env):
+    """Default evaluation (terms folded into NMO x NMO matrices) against the oracle's
+    term-order sums, on the fixture's MO grids and on seeded grids of 3000 points
+    that cover several 128-point blocks and a ragged tail."""
+    import torch
+    detci, okref, d, mo, _ = env
+    rng = numpy.random.default_rng(5)
+    rand = rng.standard_normal((4, 42, 3001))
+    for k in range(int(d["npairs"])):
+        zero, sing = detci_terms(d, k)
+        for m0, md in ((mo[0], mo[1:4]), (rand[0], rand[1:4])):
+            assert_fp64_close(detci.rho(zero, sing, m0, reference_slicing=False), okref.ci_rho(zero, sing, m0),
+                              "rho pair %d" % k)
+            assert_fp64_close(detci.jab(zero, sing, m0, md, reference_slicing=False),
+                              okref.ci_jab(zero, sing, m0, md), "jab pair %d" % k)
+            assert_fp64_close(detci.a_nabla_b(zero, sing, m0, md, reference_slicing=False),
+                              okref.ci_a_nabla_b(zero, sing, m0, md), "a_nabla_b pair %d" % k)
+    # device tensors in, device tensors out; odd MO counts (row padding of the matrices)
+    zero, sing = [[[0.5, -0.25]], [[0, 4]]], [[0.3, -0.7, 1.1], [[0, 1], [4, 2], [3, 3]]]
+    m = torch.tensor(rand[0][:5, :777], device="cuda")
+    dm = torch.tensor(rand[1:4][:, :5, :777], device="cuda")
+    r = detci.rho(zero, sing, m, reference_slicing=False)
+    assert r.is_cuda
+    assert_fp64_close(r.cpu().numpy(), okref.ci_rho(zero, sing, rand[0][:5, :777]), "rho nmo=5")
+    assert_fp64_close(detci.jab(zero, sing, m, dm, reference_slicing=False).cpu().numpy(),
+                      okref.ci_jab(zero, sing, rand[0][:5, :777], rand[1:4][:, :5, :777]), "jab nmo=5")
 
 
 def test_ci_pipeline_against_reference_data(env):
