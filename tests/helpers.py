@@ -65,3 +65,19 @@ def detci_terms(d, k):
         o += n
     sing = [[float(v) for v in d["sing_coef_%d" % k]], [[int(a), int(b)] for a, b in d["sing_pair_%d" % k]]]
     return zero, sing
+
+
+def cube_case():
+    """The Gaussian cube case (h2o_gaussian_cube.npz): the molecule with all MOs,
+    without the core MO (Gaussian's "Total SCF Density"), and the HOMO alone."""
+    qc, d = load_golden("h2o_gaussian_cube.npz")
+    dv = dict(d)
+    dv["mo_coeffs"], dv["mo_occ"] = d["mo_coeffs"][1:], d["mo_occ"][1:]
+    dh = dict(d)
+    dh["mo_coeffs"], dh["mo_occ"] = d["homo_coeffs"].reshape(1, -1), d["mo_occ"][:1]
+    return qc, from_arrays(dv), from_arrays(dh), d
+
+
+def cube_close(a, b, tol):
+    """The reference's test/tools.py equal(): allclose(a, b, rtol=100 tol, atol=tol)."""
+    numpy.testing.assert_allclose(a, b, rtol=tol * 1e2, atol=tol)

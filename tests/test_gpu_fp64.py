@@ -7,7 +7,7 @@ import ctypes
 import numpy
 import pytest
 
-from helpers import assert_fp64_close, load_golden
+from helpers import assert_fp64_close, cube_case, cube_close, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -74,6 +74,22 @@ def test_golden_reference_h2o(core):
     r2 = core.rho_compute(qc)
     assert_fp64_close(r2, d["zero"].reshape(-1), "rho vector grid")
     grid.reset_grid()
+
+
+def test_golden_gaussian_cube(core):
+    """The reference's test/grid_based/cube_files.py: H2O, spherical basis from Gaussian's
+    fchk, 3x3x3 grid through the O nucleus -- against the reference's outputs (FP64 bar)
+    and Gaussian's own cube values (that test's tolerances)."""
+    qc, qv, qh, d = cube_case()
+    kw = dict(x=d["x"], y=d["y"], z=d["z"], is_vector=False)
+    rho, drho = core.rho_compute_no_slice(qc, drv=["x", "y", "z"], **kw)
+    lapl = core.rho_compute_no_slice(qc, laplacian=True, **kw)[-1]
+    val = core.rho_compute_no_slice(qv, **kw)
+    mo = core.rho_compute_no_slice(qh, calc_mo=True, **kw)
+    for name, a, tol in (("rho", rho, 1e-5), ("drho", drho, 1e-3), ("lapl", lapl, 1e-5),
+                         ("rho_valence", val, 1e-5), ("homo", mo, 1e-5)):
+        assert_fp64_close(a, d["ref_" + name], "cube case " + name)
+        cube_close(a, d["cube_" + name], tol)
 
 
 def test_small_full_grid_vs_oracle(core):

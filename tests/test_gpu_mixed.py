@@ -147,3 +147,18 @@ def test_mixed_through_drop_in_api(mixed):
     _check(mixed, r.reshape(-1), dr.reshape(3, -1), r64.reshape(-1), dr64.reshape(3, -1), "drop-in")
     assert core.rho_compute(qc, precision="mixed").shape == r64.shape
     grid.reset_grid()
+
+
+def test_mixed_gaussian_cube(mixed):
+    """Tensor-core path on the Gaussian cube case (spherical basis from an fchk file, a
+    grid point on the O nucleus): within the mixed bar of the FP64 path and within the
+    reference test's tolerances of Gaussian's cube values."""
+    from helpers import cube_case, cube_close
+    from orbkit_gb300 import core
+    qc, _, _, d = cube_case()
+    kw = dict(x=d["x"], y=d["y"], z=d["z"], is_vector=False)
+    r, dr = core.rho_compute_no_slice(qc, drv=["x", "y", "z"], precision="mixed", **kw)
+    r64, dr64 = core.rho_compute_no_slice(qc, drv=["x", "y", "z"], **kw)
+    _check(mixed, r.reshape(-1), dr.reshape(3, -1), r64.reshape(-1), dr64.reshape(3, -1), "cube case")
+    cube_close(r, d["cube_rho"], 1e-5)
+    cube_close(dr, d["cube_drho"], 1e-3)

@@ -4,7 +4,7 @@ import numpy
 import pytest
 
 import okref
-from helpers import GOLDEN, is_x86, load_golden
+from helpers import GOLDEN, cube_case, cube_close, is_x86, load_golden
 
 DRV_ALL = [None, "x", "y", "z", "xx", "yy", "zz", "xy", "xz", "yz"]
 
@@ -197,3 +197,20 @@ def test_overlap_golden(name):
     D = numpy.array([okref.ao_dipole_matrix(qc, c) for c in "xyz"])
     _same(D, G["dip"], "dipole matrices")
     _same(okref.dipole_moment(qc, G["charges"]), G["dipole"], "dipole moment")
+
+
+def test_gaussian_cube_golden():
+    """The reference's test/grid_based/cube_files.py: H2O with a spherical basis from
+    Gaussian's fchk on a 3x3x3 grid through the O nucleus, against Gaussian's own cube
+    values (cubegen: rho, grad rho, Laplacian, valence density, HOMO) with that test's
+    tolerances, and against the reference's outputs bit for bit."""
+    qc, qv, qh, d = cube_case()
+    kw = dict(x=d["x"], y=d["y"], z=d["z"], is_vector=False)
+    rho, drho = okref.rho_compute(qc, drv=["x", "y", "z"], slice_length=0, **kw)
+    lapl = okref.rho_compute(qc, laplacian=True, slice_length=0, **kw)[-1]
+    val = okref.rho_compute(qv, slice_length=0, **kw)
+    mo = okref.rho_compute(qh, calc_mo=True, slice_length=0, **kw)
+    for name, a, tol in (("rho", rho, 1e-5), ("drho", drho, 1e-3), ("lapl", lapl, 1e-5),
+                         ("rho_valence", val, 1e-5), ("homo", mo, 1e-5)):
+        cube_close(a, d["cube_" + name], tol)
+        _same(a, d["ref_" + name], name)
