@@ -345,7 +345,7 @@ def run_ours(args):
             "kernel": "rho_mixed_kernel", "kernel_ms": kms,
             "algorithmic": "8*NMO*NAO FLOP per point (value + 3 derivatives of C.AO)",
             "hbm_bytes_per_point": 32, "hbm_gbs": 32.0 * npts / (kms * 1e-3) / 1e9, "hbm_peak_gbs": pk["hbm_gbs"],
-            "fp64_fma_peak_per_s": fma,
+            "fp64_fma_peak_per_s": fp64_fma_peak(), "fp64_fma_diag_per_s": fma,
         },
         "clocks": clk,
         "e2e": {"value": world * npts / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -363,7 +363,12 @@ def run_ours(args):
 
 def run_profile(args):
     """Minimal launch sequence for ncu: each kernel of the path once as warm-up, then
-    once more (mixed kernel, FP64 fused kernel) on the full workload."""
+    once more (mixed kernel, FP64 fused kernel) on the full workload.  With --workload
+    detci / overlap: the kernels of that row twice on a smaller case."""
+    if args.workload == "detci":
+        return _profile_detci()
+    if args.workload == "overlap":
+        return _profile_overlap()
     import torch
     from orbkit_gb300 import _lib, mixed, synthetic
     from orbkit_gb300.core import _DeviceGrid
@@ -387,6 +392,38 @@ def run_profile(args):
     torch.cuda.synchronize()
     ev.check()
     print("profile run done: %d points" % npts)
+
+
+def _profile_detci():
+    """detci kernels (quadratic forms and term order) twice each on 2^20 points of
+    seeded MO grids (42 MOs, the first state pair's terms): 1.4 GB on the device."""
+    import torch
+    from orbkit_gb300 import detci
+    d = numpy.load(os.path.join(ROOT, "tests", "golden", "h3p_detci.npz"))
+    npts = 1 << 20
+    zero = [[list(d["zero_coef_0"])], [list(int(v) for v in d["zero_orb_0"])]]
+    sing = [list(d["sing_coef_0"]), [list(map(int, p)) for p in d["sing_pair_0"]]]
+    g = torch.Generator(device="cuda").manual_seed(7)
+    mo = torch.randn((42, npts), generator=g, dtype=torch.float64, device="cuda")
+    drv = torch.randn((3, 42, npts), generator=g, dtype=torch.float64, device="cuda")
+    for exact in (False, False, True, True):
+        detci.rho(zero, sing, mo, reference_slicing=False, exact=exact)
+        detci.jab(zero, sing, mo, drv, reference_slicing=False, exact=exact)
+    torch.cuda.synchronize()
+    print("profile run done: detci, %d points" % npts)
+
+
+def _profile_overlap():
+    """okg_ao_overlap on the 200-atom basis (2420 Cartesian AOs): S and dS/dx, twice."""
+    import torch
+    from orbkit_gb300 import analytical_integrals as ai, synthetic
+    qc = synthetic.large()["qc"]
+    geo = torch.tensor(numpy.asarray(qc.geo_spec), device="cuda")
+    for _ in range(2):
+        for d in (None, "x"):
+            ai.get_ao_overlap(geo, geo, qc.ao_spec, drv=d)
+    torch.cuda.synchronize()
+    print("profile run done: overlap")
 
 
 def _events():
@@ -624,7 +661,8 @@ def _detci_workload(args, flush):
     fma_rho = sum(16 * (nmo - 16 * c) for c in range(ch)) + sum(nmo - 16 * c for c in range(ch))
     fma_jab = ch * nmo * (16 + 3)
     fma_rate = (fma_rho + fma_jab) * npts / (ms * 1e-3)
-    peak = ctypes_fp64_rate(_lib.load())
+    peak = fp64_fma_peak()
+    diag = ctypes_fp64_rate(_lib.load())
     res = {"metric": "grid points/s for the CI transition density + flux density from MO grids",
            "unit": "grid points/s", "value": npts / (ms * 1e-3), "ms_per_step": ms, "dtype": "f64",
            "config": {"workload": "detci: %d zero + %d single terms over %d MOs, %d points (rho then jab)"
@@ -634,9 +672,9 @@ def _detci_workload(args, flush):
                                      "api": "okg_ci_rho + okg_ci_jab (exact=True)"},
                       "max_normwise_diff_vs_term_order": err},
            "roofline": {"bound": "fp64", "achieved": fma_rate, "peak": peak, "unit": "FMA/s",
-                        "frac": (fma_rate / peak) if peak else None, "traffic": None,
-                        "note": "FMAs issued per point %d (rho) + %d (flux); peak = okg_diag_fp64_fma_rate"
-                                % (fma_rho, fma_jab)},
+                        "frac": fma_rate / peak, "traffic": None,
+                        "note": "FMAs issued per point %d (rho) + %d (flux); peak = 2 DFMA/clk/SM x SMs x max "
+                                "clock; the FMA-chain diagnostic reaches %.3g" % (fma_rho, fma_jab, diag or 0)},
            "gpu_launches": 2}
     if not args.no_cpu_baseline:
         okref = _oracle()
@@ -650,6 +688,20 @@ def _detci_workload(args, flush):
         res["cpu_baseline"] = {"value": n / dt, "unit": "grid points/s", "cores": 1, "kind": "port",
                                "sample": "%d points, the same terms (numpy restatement of cy_ci), %.2f s" % (n, dt)}
     return res
+
+
+def fp64_fma_peak():
+    """FP64 FMA peak of the device: 2 DFMA per clock per SM (the rate ncu shows for
+    ci_quad_kernel at 98.6 % FP64-pipe activity) x SMs x the maximum SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", "0", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=20).stdout.strip().splitlines()
+        mhz = float(out[0])
+    except Exception:
+        mhz = 2070.0
+    return 2.0 * sms * mhz * 1e6
 
 
 def ctypes_fp64_rate(L):
