@@ -32,6 +32,7 @@
 // by a second kernel: out[r, s] = sum_a sum_b k_a k_b (N_a N_b S[a, b]).
 #include <math.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "okg_internal.cuh"
@@ -72,13 +73,23 @@ __device__ __forceinline__ void os_axis(double xpa, double ab, double p, int la,
     sp = v[la];
 }
 
-__global__ void ao_overlap_kernel(int nrow, const OvRow* __restrict__ rows, const double2* __restrict__ prim,
-                                  const double* __restrict__ pnorm, const double* __restrict__ geo_a,
-                                  const double* __restrict__ geo_b, int drv, double* __restrict__ out, long long ld)
+// A warp computes 32 elements of one bra row I.  Its kets are consecutive in the
+// plan's ket order (sorted by primitive count, then exponents), so the lanes run
+// the same primitive loops and recursion lengths; a primitive pair is skipped only
+// when exp(-mu R^2) underflows for every lane (it contributes exactly 0 to the
+// others as well).
+__global__ void __launch_bounds__(256) ao_overlap_kernel(int nrow, const OvRow* __restrict__ rows,
+                                                         const int* __restrict__ ket_order,
+                                                         const double2* __restrict__ prim,
+                                                         const double* __restrict__ pnorm,
+                                                         const double* __restrict__ geo_a,
+                                                         const double* __restrict__ geo_b, int drv,
+                                                         double* __restrict__ out, long long ld)
 {
-    const int J = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Jo = blockIdx.x * blockDim.x + threadIdx.x;
     const int I = blockIdx.y * blockDim.y + threadIdx.y;
-    if (I >= nrow || J >= nrow) return;
+    if (I >= nrow || Jo >= nrow) return;
+    const int J = ket_order[Jo];
     const OvRow ri = rows[I], rj = rows[J];
     double A[3], B[3], AB[3];
     double rr = 0.0;
@@ -101,7 +112,7 @@ __global__ void ao_overlap_kernel(int nrow, const OvRow* __restrict__ rows, cons
             const double al = pa.x, be = pb.x;
             const double inv_p = 1.0 / (al + be);
             const double arg = al * be * inv_p * rr;
-            if (arg > 746.0) continue;  // exp(-arg) is 0 in double: the pair adds exactly 0
+            if (__all_sync(__activemask(), arg > 746.0)) continue;  // exp(-arg) is 0 in double: adds exactly 0
             const double eab = exp(-arg);
             const double t = M_PI * inv_p;
             const double pref = eab * t * sqrt(t);
@@ -175,6 +186,7 @@ __global__ void aoom_transform_kernel(int nout, const int* __restrict__ ptr, con
 using namespace okg;
 
 struct okg_overlap_plan {
+    int* ket_order = nullptr;  // kets sorted by (primitive count, exponents): the kernel's column order
     int natom, nshell, ncart, nprim, nout;
     int max_la, max_lb_base;
     int spherical, has_renorm;
@@ -204,6 +216,19 @@ static double ov_ao_norm(int l, int m, int n, double alpha, int is_normalized)
 
 static int ov_pack(const int* l) { return l[0] | (l[1] << 8) | (l[2] << 16); }
 
+// Kets sorted by (primitive count, packed ket exponents, row): rows a warp handles
+// together then run the same loops.
+static std::vector<int> ov_ket_order(const std::vector<OvRow>& rows)
+{
+    std::vector<int> o(rows.size());
+    for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
+    std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
+        if (rows[a].nprim != rows[b].nprim) return rows[a].nprim < rows[b].nprim;
+        return rows[a].lb < rows[b].lb;
+    });
+    return o;
+}
+
 static void ov_free(okg_overlap_plan* p)
 {
     if (!p) return;
@@ -215,6 +240,7 @@ static void ov_free(okg_overlap_plan* p)
     cudaFree(p->tcart);
     cudaFree(p->tcoef);
     cudaFree(p->work);
+    cudaFree(p->ket_order);
     delete p;
 }
 
@@ -327,7 +353,8 @@ extern "C" int okg_overlap_plan_create(int natom, int nshell, const int* h_shell
         (h_renorm && (st = ov_upload(&P->renorm, h_renorm, (size_t)ncart, "okg_overlap_plan_create"))) ||
         (st = ov_upload(&P->tptr, tptr.data(), tptr.size(), "okg_overlap_plan_create")) ||
         (st = ov_upload(&P->tcart, tcart.data(), tcart.size(), "okg_overlap_plan_create")) ||
-        (st = ov_upload(&P->tcoef, tcoef.data(), tcoef.size(), "okg_overlap_plan_create"))) {
+        (st = ov_upload(&P->tcoef, tcoef.data(), tcoef.size(), "okg_overlap_plan_create")) ||
+        (st = ov_upload(&P->ket_order, ov_ket_order(P->h_rows).data(), (size_t)ncart, "okg_overlap_plan_create"))) {
         ov_free(P);
         return st;
     }
@@ -372,8 +399,12 @@ extern "C" int okg_overlap_plan_set_ket(okg_overlap_plan* plan, const int* h_lxl
         plan->h_rows[r].lb = ov_pack(l);
     }
     plan->max_lb = max_lb;
-    return cuda_status(cudaMemcpy(plan->rows, plan->h_rows.data(), plan->h_rows.size() * sizeof(OvRow),
-                                  cudaMemcpyHostToDevice),
+    int st = cuda_status(cudaMemcpy(plan->rows, plan->h_rows.data(), plan->h_rows.size() * sizeof(OvRow),
+                                    cudaMemcpyHostToDevice),
+                         "okg_overlap_plan_set_ket");
+    if (st) return st;
+    const std::vector<int> order = ov_ket_order(plan->h_rows);
+    return cuda_status(cudaMemcpy(plan->ket_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice),
                        "okg_overlap_plan_set_ket");
 }
 
@@ -390,14 +421,15 @@ extern "C" int okg_ao_overlap(okg_overlap_plan* plan, const double* d_geo_a, con
     const bool direct = raw || (!plan->spherical && !plan->has_renorm);
     double* S = direct ? d_out : plan->work;
     const long long lds = direct ? ld : plan->ncart;
-    const dim3 blk(16, 16);
-    const dim3 grd((plan->ncart + 15) / 16, (plan->ncart + 15) / 16);
-    ao_overlap_kernel<<<grd, blk, 0, st>>>(plan->ncart, plan->rows, plan->prim, plan->pnorm, d_geo_a, d_geo_b, drv,
-                                          S, lds);
+    const dim3 blk(32, 8);
+    const dim3 grd((plan->ncart + 31) / 32, (plan->ncart + 7) / 8);
+    ao_overlap_kernel<<<grd, blk, 0, st>>>(plan->ncart, plan->rows, plan->ket_order, plan->prim, plan->pnorm, d_geo_a,
+                                          d_geo_b, drv, S, lds);
     int s = cuda_status(cudaGetLastError(), "okg_ao_overlap launch");
     if (s || direct) return s;
+    const dim3 tblk(16, 16);
     const dim3 grt((plan->nout + 15) / 16, (plan->nout + 15) / 16);
-    aoom_transform_kernel<<<grt, blk, 0, st>>>(plan->nout, plan->tptr, plan->tcart, plan->tcoef, plan->renorm, S,
+    aoom_transform_kernel<<<grt, tblk, 0, st>>>(plan->nout, plan->tptr, plan->tcart, plan->tcoef, plan->renorm, S,
                                                lds, d_out, ld);
     return cuda_status(cudaGetLastError(), "okg_ao_overlap transform launch");
 }
