@@ -26,8 +26,11 @@
 // Tile: 128 grid points (the MMA's M), N = MO block padded to a multiple of 16
 // (<= 64 per pass), K = canonical Cartesian AO columns in chunks of 32 (one
 // 64-byte swizzle row of BF16).  Persistent CTAs, one per SM, each with
-// 128 x NG generation threads (NG threads per grid point) and one MMA warp,
-// connected by a two-stage ring in shared memory:
+// 128 x NG generation threads (NG threads per grid point), one MMA warp and one
+// tile warp.  The tile warp takes tiles from a device counter and screens them up
+// to two tiles ahead (double-buffered tile index, descriptor and screening tables,
+// handed over through "screened" and "kfree" mbarriers).  Generation threads and
+// the MMA warp are connected by a two-stage ring in shared memory:
 //   * generation threads write 4 channels x 3 parts of A (128 x 32 BF16, K-major,
 //     SWIZZLE_64B) for a chunk into a free stage and arrive on its "full" barrier;
 //   * the MMA warp bulk-copies the chunk's pre-split, pre-swizzled B block into the
@@ -288,13 +291,11 @@ struct CtaState {
     uint32_t bar_bload;          // NSTAGE mbarriers: the stage's B block has landed (bulk copy)
     uint32_t bar_acc_full;       // accumulators of a job (tile, MO pass) complete (tcgen05.commit)
     uint32_t bar_acc_empty;      // every generation thread has read the accumulators
-    uint32_t bar_screened;       // 2 mbarriers (tile buffers): tile index and column masks written
-    uint32_t bar_kfree;          // 2 mbarriers: the MMA warp is done with the buffer's tile
+    uint32_t bar_screened;       // 2 mbarriers (tile buffers): tile index and screening tables written
+    uint32_t bar_kfree;          // 2 mbarriers: generation threads and MMA warp are done with the buffer's tile
     uint32_t tmem;
     int* abort_flag;
-    float* bbox;                 // lo x,y,z, hi x,y,z of the tile being screened
-    float* bbox_part;            // 4 warps x 6
-    unsigned char* nkeep;        // per shell: primitives kept for the tile being generated
+    unsigned char* nkeep;        // 2 x MAX_SHELLS: per shell, primitives kept for the buffer's tile
     unsigned* kmask;             // 2 x MAX_CHUNKS: per chunk, columns whose shell is kept for the buffer's tile
     long long* tile_slot;        // 2: tile of the buffer (local to its molecule); -1: no more tiles
     MolDesc* mol;                // 2: molecule of the buffer's tile (one copy for the single-molecule kernel)
@@ -385,13 +386,6 @@ __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int
     return true;
 }
 
-// Generation threads only: a named barrier (id 1) over the 128 NG generation threads.
-template <int NTG>
-__device__ __forceinline__ void gen_sync()
-{
-    asm volatile("bar.sync 1, %0;" ::"r"(NTG) : "memory");
-}
-
 // K-steps (16 columns each) of a kept chunk that hold a kept column: the MMAs of a
 // K-step whose columns are all screened are not issued.
 __device__ __forceinline__ int ksteps_of(unsigned km)
@@ -416,33 +410,30 @@ struct TileFeed {
     int nmol, grab;
 };
 
-// Generation threads: take the next tile into buffer `ord` % 2 (once the MMA warp
-// has released the buffer's previous tile), this thread's point of it, the tile's
-// bounding box and the screening of every shell against it; then each thread
-// arrives on the buffer's "screened" barrier.  Returns the tile (local to its
-// molecule) or -1 when there are no more.
 // Grid points of a generation thread: P consecutive rows of the tile.
 template <int P>
 struct GenPts {
     double x[P], y[P], z[P];
 };
 
-template <int NTG, int P, bool BATCH>
-__device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const CtaState& S, uint32_t ord,
-                                                      long long& gnext, long long& gend, long long& gpend,
-                                                      long long& p, bool& valid, GenPts<P>& gp, int* status)
+// Tile warp (the last warp of the CTA): takes tiles from the feed into buffer
+// ord % 2 once the generation threads and the MMA warp have released that buffer's
+// previous tile, computes the tile's bounding box and screens every shell against
+// it (primitives kept per shell, kept columns per chunk), then arrives on the
+// buffer's "screened" barrier.  It runs up to two tiles ahead of the generation
+// threads, so none of this is on their path.  A buffer with tile -1 ends the CTA.
+template <bool BATCH>
+__device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, int* status)
 {
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int b = ord & 1;
-    if (ord >= 2 && !mbar_wait(S.bar_kfree + 8 * b, ((ord >> 1) - 1) & 1u, status)) *S.abort_flag = 1;
-    // every generation thread is done with the buffer's previous tile (its epilogue
-    // and stores read the buffer's descriptor) before warp 0 overwrites it
-    gen_sync<NTG>();
-    if (warp == 0) {
+    const int lane = threadIdx.x & 31;
+    long long gnext = 0, gend = 0, gpend = -1;
+    for (uint32_t ord = 0;; ++ord) {
+        const int b = ord & 1;
+        if (ord >= 2 && !mbar_wait(S.bar_kfree + 8 * b, ((ord >> 1) - 1) & 1u, status)) *S.abort_flag = 1;
         long long t = -1;
         int mol = 0;
         // the counter increment for the following tile (or range) is issued one
-        // fetch ahead (gpend, thread 0 only), so its round trip overlaps a tile
+        // fetch ahead (gpend), so its round trip overlaps a tile
         if (lane == 0 && !*S.abort_flag) {
             if (!BATCH) {
                 t = gpend >= 0 ? gpend : (long long)atomicAdd(F.counter, 1ull);
@@ -467,50 +458,40 @@ __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const C
                 }
             }
         }
-        if (BATCH) {
-            t = __shfl_sync(0xffffffffu, t, 0);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (BATCH && t >= 0) {
             mol = __shfl_sync(0xffffffffu, mol, 0);
-            if (t >= 0) {
-                constexpr int U = (int)(sizeof(MolDesc) / 16);
-                const uint4* src = (const uint4*)(F.descs + mol);
-                uint4* dst = (uint4*)(S.mol + b);
-                for (int i = lane; i < U; i += 32) dst[i] = src[i];
-                if (lane == 0) t -= F.descs[mol].tile0;
-            }
+            constexpr int U = (int)(sizeof(MolDesc) / 16);
+            const uint4* src = (const uint4*)(F.descs + mol);
+            uint4* dst = (uint4*)(S.mol + b);
+            for (int i = lane; i < U; i += 32) dst[i] = src[i];
+            t -= F.descs[mol].tile0;
         }
         if (lane == 0) S.tile_slot[b] = t;
-    }
-    gen_sync<NTG>();
-    const long long tile = S.tile_slot[b];
-    if (tile < 0) {
-        mbar_arrive(S.bar_screened + 8 * b);
-        return -1;
-    }
-    const MolDesc& D = S.mol[BATCH ? b : 0];
-    const BasisDev& B = D.B;
-    // the point this thread stores (TMEM lane 32 (warp % 4) + lane of the epilogue)
-    valid = tile_point(D, tile, 32 * (warp & 3) + lane, p);
-    // the points this thread generates: rows P (tid % (128 / P)) + i
-    float v[6] = {3.0e38f, 3.0e38f, 3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};
-#pragma unroll
-    for (int i = 0; i < P; ++i) {
-        long long pg;
-        const bool vg = tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
-        grid_point(D.g, pg, gp.x[i], gp.y[i], gp.z[i]);
-        if (vg) {
-            const float fx = dbl_to_flt_rn(gp.x[i]), fy = dbl_to_flt_rn(gp.y[i]), fz = dbl_to_flt_rn(gp.z[i]);
-            v[0] = fminf(v[0], fx);
-            v[1] = fminf(v[1], fy);
-            v[2] = fminf(v[2], fz);
-            v[3] = fmaxf(v[3], fx);
-            v[4] = fmaxf(v[4], fy);
-            v[5] = fmaxf(v[5], fz);
+        __syncwarp();
+        if (t < 0) {
+            mbar_arrive(S.bar_screened + 8 * b);
+            return;
         }
-    }
-    unsigned* km = S.kmask + b * MAX_CHUNKS;
-    // bounding box of the tile's valid points (generation group 0 = warps 0 .. 4 / P - 1)
-    constexpr int BW = 4 / P;
-    if (warp < BW) {
+        const MolDesc& D = S.mol[BATCH ? b : 0];
+        const BasisDev& B = D.B;
+        // bounding box of the tile's valid points (four rows per lane)
+        float v[6] = {3.0e38f, 3.0e38f, 3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+        for (int i = 0; i < M / 32; ++i) {
+            long long pg;
+            if (tile_point(D, t, lane + 32 * i, pg)) {
+                double x, y, z;
+                grid_point(D.g, pg, x, y, z);
+                const float fx = dbl_to_flt_rn(x), fy = dbl_to_flt_rn(y), fz = dbl_to_flt_rn(z);
+                v[0] = fminf(v[0], fx);
+                v[1] = fminf(v[1], fy);
+                v[2] = fminf(v[2], fz);
+                v[3] = fmaxf(v[3], fx);
+                v[4] = fmaxf(v[4], fy);
+                v[5] = fmaxf(v[5], fz);
+            }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
@@ -518,34 +499,53 @@ __device__ __forceinline__ long long fetch_and_screen(const TileFeed& F, const C
 #pragma unroll
             for (int c = 3; c < 6; ++c) v[c] = fmaxf(v[c], __shfl_xor_sync(0xffffffffu, v[c], o));
         }
-        if (lane == 0)
-            for (int c = 0; c < 6; ++c) S.bbox_part[warp * 6 + c] = v[c];
+        unsigned* km = S.kmask + b * MAX_CHUNKS;
+        unsigned char* nkeep = S.nkeep + b * MAX_SHELLS;
+        for (int c = lane; c < B.nmchunk; c += 32) km[c] = 0u;
+        __syncwarp();
+        // a primitive is kept while alpha log2(e) d^2 <= SCREEN_LOG2 (primitives sorted by alpha per shell)
+        for (int si = lane; si < B.nshell; si += 32) {
+            const Shell sh = load_shell(B.shells + si);
+            const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
+                        az = (float)B.atoms[4 * sh.atom + 2];
+            const float dx = fmaxf(0.f, fmaxf(v[0] - ax, ax - v[3]));
+            const float dy = fmaxf(0.f, fmaxf(v[1] - ay, ay - v[4]));
+            const float dz = fmaxf(0.f, fmaxf(v[2] - az, az - v[5]));
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            int nk = 0;
+            while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+            nkeep[si] = (unsigned char)nk;
+            if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
+        }
+        __syncwarp();
+        mbar_arrive(S.bar_screened + 8 * b);
     }
-    for (int c = tid; c < B.nmchunk; c += NTG) km[c] = 0u;
-    gen_sync<NTG>();
-    if (tid < 6) {
-        float a = S.bbox_part[tid];
-        for (int w = 1; w < BW; ++w)
-            a = tid < 3 ? fminf(a, S.bbox_part[w * 6 + tid]) : fmaxf(a, S.bbox_part[w * 6 + tid]);
-        S.bbox[tid] = a;
+}
+
+// Generation threads: wait until buffer ord % 2 holds a screened tile; this
+// thread's store point (TMEM lane 32 (warp % 4) + lane of the epilogue) and its
+// generation points (rows P (tid % (128 / P)) + i).  Returns the tile (local to its
+// molecule) or -1 when there are no more.
+template <int P, bool BATCH>
+__device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t ord, long long& p, bool& valid,
+                                                   GenPts<P>& gp, int* status)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int b = ord & 1;
+    if (!mbar_wait(S.bar_screened + 8 * b, (ord >> 1) & 1u, status)) {
+        *S.abort_flag = 1;
+        return -1;
     }
-    gen_sync<NTG>();
-    // a primitive is kept while alpha log2(e) d^2 <= SCREEN_LOG2 (primitives sorted by alpha per shell)
-    for (int si = tid; si < B.nshell; si += NTG) {
-        const Shell sh = load_shell(B.shells + si);
-        const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
-                    az = (float)B.atoms[4 * sh.atom + 2];
-        const float dx = fmaxf(0.f, fmaxf(S.bbox[0] - ax, ax - S.bbox[3]));
-        const float dy = fmaxf(0.f, fmaxf(S.bbox[1] - ay, ay - S.bbox[4]));
-        const float dz = fmaxf(0.f, fmaxf(S.bbox[2] - az, az - S.bbox[5]));
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        int nk = 0;
-        while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
-        S.nkeep[si] = (unsigned char)nk;
-        if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
+    const long long tile = S.tile_slot[b];
+    if (tile < 0) return -1;
+    const MolDesc& D = S.mol[BATCH ? b : 0];
+    valid = tile_point(D, tile, 32 * (warp & 3) + lane, p);
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+        long long pg;
+        tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
+        grid_point(D.g, pg, gp.x[i], gp.y[i], gp.z[i]);
     }
-    gen_sync<NTG>();
-    mbar_arrive(S.bar_screened + 8 * b);
     return tile;
 }
 
@@ -610,8 +610,9 @@ __device__ __forceinline__ void shell_eval2_L(int L, const float (&X)[2], const 
 // With P = 2 the two points are adjacent in the M-major tile: each part of a
 // value pair is one packed conversion and one 4-byte store.
 template <int NTG, int P>
-__device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaState& S, uint32_t& seq, AtomRun<P>& ar,
-                                          unsigned chmask, const GenPts<P>& gp, int* status)
+__device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char* nkeep, int c, const CtaState& S,
+                                          uint32_t& seq, AtomRun<P>& ar, unsigned chmask, const GenPts<P>& gp,
+                                          int* status)
 {
     constexpr int NG = NTG * P / 128;  // generation groups
     const int tid = threadIdx.x;
@@ -642,7 +643,7 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, int c, const CtaSta
             }
         }
         if (!ar.mine) continue;
-        const int nk = S.nkeep[si];
+        const int nk = nkeep[si];
         if (nk == 0) continue;
         if constexpr (P == 1) {
             // primitives two at a time (two independent exponentials in flight)
@@ -769,17 +770,16 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
 // generated before the epilogue of the current job, so the tensor core's tail
 // of a job overlaps useful work.
 template <int NTG, int P, bool BATCH>
-__device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, int* status)
+__device__ __forceinline__ void gen_role(const CtaState& S, int* status)
 {
     constexpr int E = NTG / 128;  // epilogue warps per TMEM lane quarter
     const int warp = threadIdx.x >> 5;
     const int h = warp >> 2;
     uint32_t seq = 0, accseq = 0, ord = 0;
-    long long gnext = 0, gend = 0, gpend = -1;
     long long p = 0;
     bool valid = false;
     GenPts<P> gp;
-    if (fetch_and_screen<NTG, P, BATCH>(F, S, ord, gnext, gend, gpend, p, valid, gp, status) < 0) return;
+    if (gen_open_tile<P, BATCH>(S, ord, p, valid, gp, status) < 0) return;
     int gpass = 0;
     AtomRun<P> ar;
     int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
@@ -791,8 +791,9 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
         {
             const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
             const BasisDev& B = Dg.B;
+            const unsigned char* nkeep = S.nkeep + (ord & 1) * MAX_SHELLS;
             while (c >= 0) {
-                gen_chunk<NTG, P>(B, c, S, seq, ar, chmask, gp, status);
+                gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
                 ++nch;
                 nks += ksteps_of(km[c]);
                 c = next_kept(km, B.nmchunk, c);
@@ -806,8 +807,7 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
         if (npass_next == Dg.npass) {
             ord_next = ord + 1;
             npass_next = 0;
-            more = fetch_and_screen<NTG, P, BATCH>(F, S, ord_next, gnext, gend, gpend, p_next, valid_next, gp,
-                                                   status) >= 0;
+            more = gen_open_tile<P, BATCH>(S, ord_next, p_next, valid_next, gp, status) >= 0;
         }
         int c_next = -1, nch_next = 0, nks_next = 0;
         if (more) {
@@ -816,7 +816,8 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
             ar = AtomRun<P>();
             c_next = next_kept(kmn, Dn.B.nmchunk, -1);
             if (c_next >= 0) {
-                gen_chunk<NTG, P>(Dn.B, c_next, S, seq, ar, Dn.want_grad ? 0xFu : 0x1u, gp, status);
+                gen_chunk<NTG, P>(Dn.B, S.nkeep + (ord_next & 1) * MAX_SHELLS, c_next, S, seq, ar,
+                                  Dn.want_grad ? 0xFu : 0x1u, gp, status);
                 ++nch_next;
                 nks_next += ksteps_of(kmn[c_next]);
                 c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
@@ -835,6 +836,8 @@ __device__ __forceinline__ void gen_role(const TileFeed& F, const CtaState& S, i
             }
 #pragma unroll
             for (int o = 0; o < 4; ++o) acc[o] = 0.0;
+            // this thread is done with the tile's buffer (descriptor, screening tables)
+            mbar_arrive(S.bar_kfree + 8 * (ord & 1));
         }
         if (!more) break;
         gpass = npass_next;
@@ -1049,9 +1052,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
     S.tile_slot = (long long*)(bar + 12);
     uint32_t* tmem_slot = (uint32_t*)(S.tile_slot + 2);
     S.abort_flag = (int*)(tmem_slot + 1);
-    S.bbox = (float*)(S.abort_flag + 1);
-    S.bbox_part = S.bbox + 6;
-    S.nkeep = (unsigned char*)(S.bbox_part + 24);
+    S.nkeep = (unsigned char*)(S.abort_flag + 1);
     S.mol = mol;
     S.bar_full = smem_u32(bar);
     S.bar_empty = smem_u32(bar + 2);
@@ -1070,8 +1071,8 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
         mbar_init(S.bar_acc_full, 1);
         mbar_init(S.bar_acc_empty, NTG);
         for (int b = 0; b < 2; ++b) {
-            mbar_init(S.bar_screened + 8 * b, NTG);
-            mbar_init(S.bar_kfree + 8 * b, 1);
+            mbar_init(S.bar_screened + 8 * b, 32);     // the tile warp
+            mbar_init(S.bar_kfree + 8 * b, NTG + 1);   // every generation thread and the MMA warp
         }
         *S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1091,7 +1092,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
 constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * 2 * MAX_CHUNKS + 12 * 8 + 2 * 8 + 4 + 4 +
-                              4 * 6 + 4 * 24 + MAX_SHELLS + 64;
+                              2 * MAX_SHELLS + 64;
 static_assert(SMEM_BYTES + 2 * sizeof(MolDesc) <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 static_assert(KC == 32, "column masks are 32-bit and operand rows one 64-byte swizzle row");
 static_assert(sizeof(MolDesc) % 16 == 0, "descriptors are copied in 16-byte units");
@@ -1150,14 +1151,17 @@ inline void make_desc(MolDesc& D, const BasisDev& B, const Grid& g, const void* 
 extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
 
 // Single molecule: its descriptor is copied to shared memory once.
+// Threads of a CTA: NTG generation threads, the MMA warp and the tile warp.
+__host__ __device__ constexpr int cta_threads(int ntg) { return ntg + 64; }
+
 template <int NTG, int PP>
-__global__ void __launch_bounds__(NTG + 32, 1) rho_mixed_kernel(const __grid_constant__ Params P)
+__global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_kernel(const __grid_constant__ Params P)
 {
     __shared__ MolDesc mol[1];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
     if (threadIdx.x < sizeof(MolDesc) / 16) ((uint4*)mol)[threadIdx.x] = ((const uint4*)&P.D)[threadIdx.x];
     const uint32_t tm_cols = tmem_cols_for(P.D.npad);
-    CtaState S = cta_setup<NTG + 32, NTG>(smem, mol, tm_cols);
+    CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, tm_cols);
     TileFeed F;
     F.counter = P.counter;
     F.ntiles = P.D.ntiles;
@@ -1165,9 +1169,11 @@ __global__ void __launch_bounds__(NTG + 32, 1) rho_mixed_kernel(const __grid_con
     F.nmol = 1;
     F.grab = 1;
     if (threadIdx.x < NTG)
-        gen_role<NTG, PP, false>(F, S, P.status);
-    else
+        gen_role<NTG, PP, false>(S, P.status);
+    else if (threadIdx.x < NTG + 32)
         mma_role<false>(S, P.status);
+    else
+        tile_role<false>(F, S, P.status);
     cta_teardown(S, tm_cols);
 }
 
@@ -1185,11 +1191,11 @@ struct BatchParams {
 };
 
 template <int NTG, int PP>
-__global__ void __launch_bounds__(NTG + 32, 1) rho_mixed_batch_kernel(const BatchParams P)
+__global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(const BatchParams P)
 {
     __shared__ MolDesc mol[2];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    CtaState S = cta_setup<NTG + 32, NTG>(smem, mol, 512);
+    CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, 512);
     TileFeed F;
     F.counter = P.counter;
     F.ntiles = P.total_tiles;
@@ -1197,9 +1203,11 @@ __global__ void __launch_bounds__(NTG + 32, 1) rho_mixed_batch_kernel(const Batc
     F.nmol = P.nmol;
     F.grab = P.grab;
     if (threadIdx.x < NTG)
-        gen_role<NTG, PP, true>(F, S, P.status);
-    else
+        gen_role<NTG, PP, true>(S, P.status);
+    else if (threadIdx.x < NTG + 32)
         mma_role<true>(S, P.status);
+    else
+        tile_role<true>(F, S, P.status);
     cta_teardown(S, 512);
 }
 
@@ -1296,22 +1304,22 @@ static cudaError_t configure_kernels()
 static void launch_single(int layout, unsigned grid, cudaStream_t st, const Params& P)
 {
     switch (layout) {
-    case 0: rho_mixed_kernel<256, 1><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
-    case 2: rho_mixed_kernel<512, 1><<<grid, 512 + 32, SMEM_BYTES, st>>>(P); break;
-    case 3: rho_mixed_kernel<256, 2><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
-    case 4: rho_mixed_kernel<384, 2><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
-    default: rho_mixed_kernel<384, 1><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
+    case 0: rho_mixed_kernel<256, 1><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 2: rho_mixed_kernel<512, 1><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
+    case 3: rho_mixed_kernel<256, 2><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 4: rho_mixed_kernel<384, 2><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+    default: rho_mixed_kernel<384, 1><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
     }
 }
 
 static void launch_batch(int layout, unsigned grid, cudaStream_t st, const BatchParams& P)
 {
     switch (layout) {
-    case 0: rho_mixed_batch_kernel<256, 1><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
-    case 2: rho_mixed_batch_kernel<512, 1><<<grid, 512 + 32, SMEM_BYTES, st>>>(P); break;
-    case 3: rho_mixed_batch_kernel<256, 2><<<grid, 256 + 32, SMEM_BYTES, st>>>(P); break;
-    case 4: rho_mixed_batch_kernel<384, 2><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
-    default: rho_mixed_batch_kernel<384, 1><<<grid, 384 + 32, SMEM_BYTES, st>>>(P); break;
+    case 0: rho_mixed_batch_kernel<256, 1><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 2: rho_mixed_batch_kernel<512, 1><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
+    case 3: rho_mixed_batch_kernel<256, 2><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 4: rho_mixed_batch_kernel<384, 2><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+    default: rho_mixed_batch_kernel<384, 1><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
     }
 }
 }  // namespace mx
