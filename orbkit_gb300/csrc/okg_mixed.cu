@@ -799,6 +799,11 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
                 c = next_kept(km, B.nmchunk, c);
             }
         }
+        // single molecule: the tile's screening tables are not read after its last
+        // chunk, so the buffer is released now and the tile warp screens ahead
+        // during this job's epilogue (a batch releases after the stores: the buffer
+        // also holds the molecule's descriptor)
+        if (!BATCH && gpass == Dg.npass - 1) mbar_arrive(S.bar_kfree + 8 * (ord & 1));
         // the next job: the next MO pass of this tile, or pass 0 of a new tile
         int npass_next = gpass + 1;
         uint32_t ord_next = ord;
@@ -837,7 +842,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
 #pragma unroll
             for (int o = 0; o < 4; ++o) acc[o] = 0.0;
             // this thread is done with the tile's buffer (descriptor, screening tables)
-            mbar_arrive(S.bar_kfree + 8 * (ord & 1));
+            if (BATCH) mbar_arrive(S.bar_kfree + 8 * (ord & 1));
         }
         if (!more) break;
         gpass = npass_next;
