@@ -707,7 +707,7 @@ def fp64_fma_peak():
 def ctypes_fp64_rate(L):
     import ctypes
     v = ctypes.c_double(0)
-    if L.okg_diag_fp64_fma_rate(20000, ctypes.byref(v)) != 0:
+    if L.okg_diag_fp64_fma_rate(4000, ctypes.byref(v)) != 0:
         return None
     return v.value
 
