@@ -136,6 +136,7 @@ __device__ __forceinline__ Radial<double> radial64(const double* __restrict__ pr
     Radial<double> r{0.0, 0.0, 0.0};
     for (int q = 0; q < np; ++q) {
         const double a = prim[2 * (p0 + q)];
+        if (a * rr > 746.0) continue;  // exp(-a rr) is 0 in double: the primitive adds exactly 0
         const double w = prim[2 * (p0 + q) + 1];
         const double e = w * exp(-a * rr);
         r.R0 += e;
