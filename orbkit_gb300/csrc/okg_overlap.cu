@@ -188,7 +188,7 @@ using namespace okg;
 struct okg_overlap_plan {
     int* ket_order = nullptr;  // kets sorted by (primitive count, exponents): the kernel's column order
     int natom, nshell, ncart, nprim, nout;
-    int max_la, max_lb_base;
+    int max_la;
     int spherical, has_renorm;
     std::vector<OvRow> h_rows;
     std::vector<int> h_lxa;  // ncart x 3 (bra)
@@ -267,7 +267,6 @@ extern "C" int okg_overlap_plan_create(int natom, int nshell, const int* h_shell
     okg_overlap_plan* P = new okg_overlap_plan();
     P->natom = natom;
     P->nshell = nshell;
-    cudaGetDevice(&P->device);
     int ncart = 0, nprim = 0, nrp = 0, max_l = 0;
     for (int s = 0; s < nshell; ++s) {
         const int nc = h_shell_ncart[s], np = h_shell_nprim[s], at = h_shell_atom[s];
@@ -339,6 +338,7 @@ extern "C" int okg_overlap_plan_create(int natom, int nshell, const int* h_shell
             tcoef.push_back(1.0);
         }
     }
+    cudaGetDevice(&P->device);
     P->ncart = ncart;
     P->nprim = nprim;
     P->nout = nsph > 0 ? nsph : ncart;

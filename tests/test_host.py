@@ -74,6 +74,41 @@ def test_compute_entry_points_reject_null(lib):
                        None) == -1
 
 
+def _overlap_plan(lib, lxlylz, ncart, nprim=None, atoms=None, natom=1):
+    ip = lambda a: (ctypes.c_int * len(a))(*a)
+    nshell = len(ncart)
+    nprim = nprim or [1] * nshell
+    atoms = atoms or [0] * nshell
+    flat = [v for row in lxlylz for v in row]
+    prim = (ctypes.c_double * (2 * sum(nprim)))(*([1.0, 1.0] * sum(nprim)))
+    h = ctypes.c_void_p()
+    lib.okg_overlap_plan_create.restype = ctypes.c_int
+    return lib.okg_overlap_plan_create(natom, nshell, ip(atoms), ip(ncart), ip(nprim), ip(flat), 0, prim, None, 0,
+                                       None, None, None, ctypes.byref(h))
+
+
+def test_overlap_and_ci_validation_errors(lib):
+    """AO overlap plan and the detCI quadratic forms: bad arguments are rejected before
+    any device work."""
+    lib.okg_last_error.restype = ctypes.c_char_p
+    assert _overlap_plan(lib, [(0, 0, 0)], [1], atoms=[2], natom=2) == -1
+    assert _overlap_plan(lib, [(-1, 0, 0)], [1]) == -2
+    assert _overlap_plan(lib, [(40, 0, 0)], [1]) == -2
+    assert b"too large" in lib.okg_last_error()
+    assert _overlap_plan(lib, [(0, 0, 0)], [0]) == -1
+    lib.okg_ao_overlap.restype = ctypes.c_int
+    assert lib.okg_ao_overlap(None, None, None, 0, 0, None, ctypes.c_int64(1), None) == -1
+    lib.okg_overlap_plan_set_ket.restype = ctypes.c_int
+    assert lib.okg_overlap_plan_set_ket(None, None) == -1
+    lib.okg_ci_rho_matrix.restype = ctypes.c_int
+    assert lib.okg_ci_rho_matrix(ctypes.c_int64(10), None, ctypes.c_int64(10), 4, None, None, None) == -1
+    lib.okg_ci_flux_matrix.restype = ctypes.c_int
+    assert lib.okg_ci_flux_matrix(ctypes.c_int64(10), None, None, ctypes.c_int64(10), 4, None, ctypes.c_double(1.0),
+                                  None, None) == -1
+    lib.okg_ci_rho.restype = ctypes.c_int
+    assert lib.okg_ci_rho(ctypes.c_int64(-1), None, ctypes.c_int64(0), 0, None, None, 0, None, None, None, None) == -1
+
+
 def test_validate_drv_and_tables():
     from orbkit_gb300 import tools
     assert [tools.validate_drv(d) for d in [None, "x", "y", "z", "xx", "yy", "zz", "xy", "xz", "yz"]] == list(range(10))
