@@ -168,15 +168,29 @@ __device__ __forceinline__ void fence_proxy_async()
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8])
 {
-    uint32_t r[8];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
+
+// tcgen05.wait::ld with the destination registers of the preceding loads as
+// read-write operands: no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait_ld5(uint32_t (&r)[5][8])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[0][4]), "+r"(r[0][5]), "+r"(r[0][6]), "+r"(r[0][7]), "+r"(r[1][0]), "+r"(r[1][1]), "+r"(r[1][2]), "+r"(r[1][3]), "+r"(r[1][4]), "+r"(r[1][5]), "+r"(r[1][6]), "+r"(r[1][7]), "+r"(r[2][0]), "+r"(r[2][1]), "+r"(r[2][2]), "+r"(r[2][3]), "+r"(r[2][4]), "+r"(r[2][5]), "+r"(r[2][6]), "+r"(r[2][7]), "+r"(r[3][0]), "+r"(r[3][1]), "+r"(r[3][2]), "+r"(r[3][3]), "+r"(r[3][4]), "+r"(r[3][5]), "+r"(r[3][6]), "+r"(r[3][7]), "+r"(r[4][0]), "+r"(r[4][1]), "+r"(r[4][2]), "+r"(r[4][3]), "+r"(r[4][4]), "+r"(r[4][5]), "+r"(r[4][6]), "+r"(r[4][7]));
+}
+
+// tcgen05.wait::ld with the destination registers of the preceding loads as
+// read-write operands: no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait_ld1(uint32_t (&r)[1][8])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[0][4]), "+r"(r[0][5]), "+r"(r[0][6]), "+r"(r[0][7]));
+}
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Exact conversion of a double to float by truncating the mantissa (integer ops
@@ -726,13 +740,19 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
         int mo_end = D.nmo - pass * npad;
         mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
         for (int m0 = 0; m0 < mo_end; m0 += 8) {
+            uint32_t q[5][8];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) tmem_ld8(tl + k * npad + m0, q[k]);
+            tmem_wait_ld5(q);
             float v[8], a1[8], a2[8], a3[8], lo[8];
-            tmem_ld8(tl + 0 * npad + m0, v);
-            tmem_ld8(tl + 1 * npad + m0, a1);
-            tmem_ld8(tl + 2 * npad + m0, a2);
-            tmem_ld8(tl + 3 * npad + m0, a3);
-            tmem_ld8(tl + 4 * npad + m0, lo);
-            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                v[i] = __uint_as_float(q[0][i]);
+                a1[i] = __uint_as_float(q[1][i]);
+                a2[i] = __uint_as_float(q[2][i]);
+                a3[i] = __uint_as_float(q[3][i]);
+                lo[i] = __uint_as_float(q[4][i]);
+            }
             if (nlead < 4) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
@@ -751,9 +771,12 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
 #pragma unroll
             for (int o = 1; o < 4; ++o) {
                 if (!own[o]) continue;
+                uint32_t qd[1][8];
+                tmem_ld8(tl + (4 + o) * npad + m0, qd[0]);
+                tmem_wait_ld1(qd);
                 float vd[8];
-                tmem_ld8(tl + (4 + o) * npad + m0, vd);
-                tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 8; ++i) vd[i] = __uint_as_float(qd[0][i]);
                 DF sd;
 #pragma unroll
                 for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
