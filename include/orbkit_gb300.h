@@ -128,7 +128,10 @@ int okg_rho(const okg_basis* basis, const okg_grid* grid, int nmo, const double*
  * (orbkit/core.py:266-300), within the error stated by the tests.
  * A plan holds the tensor-core operand form of the MO coefficients. */
 typedef struct okg_mixed_plan okg_mixed_plan;
-/* Allocates the plan's device buffer (split coefficients, occupations, status word). */
+/* Allocates the plan's device buffer (split coefficients, occupations, status word).
+ * OKG_ERR_UNSUPPORTED for bases beyond the kernel's shared-memory tables: more than
+ * 2048 shells, 256 column chunks or 31 primitives in a shell (the FP64 path has no
+ * such limits). */
 int okg_mixed_plan_create(const okg_basis* basis, int nmo, okg_mixed_plan** out);
 /* Same with the MMA's N tile (MO columns per pass over the AO chunks) limited to
  * n_max (16, 32, 48 or 64; okg_mixed_plan_create uses 64): a tile shape for the

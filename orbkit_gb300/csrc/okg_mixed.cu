@@ -309,7 +309,7 @@ struct CtaState {
     uint32_t bar_kfree;          // 2 mbarriers: generation threads and MMA warp are done with the buffer's tile
     uint32_t tmem;
     int* abort_flag;
-    unsigned char* nkeep;        // 2 x MAX_SHELLS: per shell, primitives kept for the buffer's tile
+    unsigned char* nkeep;        // 2 x MAX_SHELLS: per shell, kept primitives | owning generation group << 5
     unsigned* kmask;             // 2 x MAX_CHUNKS: per chunk, columns whose shell is kept for the buffer's tile
     long long* tile_slot;        // 2: tile of the buffer (local to its molecule); -1: no more tiles
     MolDesc* mol;                // 2: molecule of the buffer's tile (one copy for the single-molecule kernel)
@@ -319,6 +319,11 @@ struct CtaState {
 // MAX_CHUNKS chunks per molecule on the mixed path.
 constexpr int MAX_SHELLS = 2048;
 constexpr int MAX_CHUNKS = 256;
+// A shell's byte of the screening table: kept primitives (low 5 bits, so at most
+// MAX_PRIM per shell on the mixed path) and the generation group that evaluates
+// the shell for this tile (high 3 bits, at most 8 groups).
+constexpr int MAX_PRIM = 31;
+constexpr int KEEP_BITS = 5;
 
 // FP64 <-> FP32 without the FP64 pipe: rounding double -> float and exact
 // float -> double through integer operations on the IEEE bit patterns.
@@ -436,9 +441,10 @@ struct GenPts {
 // it (primitives kept per shell, kept columns per chunk), then arrives on the
 // buffer's "screened" barrier.  It runs up to two tiles ahead of the generation
 // threads, so none of this is on their path.  A buffer with tile -1 ends the CTA.
-template <bool BATCH>
+template <int NG, bool BATCH>
 __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, int* status)
 {
+    static_assert(NG >= 1 && NG <= (256 >> KEEP_BITS), "generation group index must fit the screening byte");
     const int lane = threadIdx.x & 31;
     long long gnext = 0, gend = 0, gpend = -1;
     for (uint32_t ord = 0;; ++ord) {
@@ -532,6 +538,37 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
             if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
         }
         __syncwarp();
+        // generation groups: per kept chunk, each kept shell goes to the group with the
+        // least estimated work so far (kept primitives and components), so every group
+        // finishes the chunk at about the same time -- the stage's "full" barrier waits
+        // for all of them.  A group recomputes an atom's coordinates only when its
+        // previous shell belonged to another atom.
+        const int wcomp = D.want_grad ? 16 : 5;
+        for (int c = lane; c < B.nmchunk; c += 32) {
+            if (km[c] == 0u) continue;
+            const int4 ck = B.mchunks[c];
+            int load[NG];
+#pragma unroll
+            for (int g = 0; g < NG; ++g) load[g] = 0;
+#pragma unroll 4
+            for (int si = ck.x; si < ck.y; ++si) {
+                const int nk = nkeep[si];
+                if (nk == 0) continue;
+                const int w = 3 * nk + wcomp * ncanon(B.shells[si].L);
+                int gbest = 0, lbest = load[0];
+#pragma unroll
+                for (int g = 1; g < NG; ++g)
+                    if (load[g] < lbest) {
+                        lbest = load[g];
+                        gbest = g;
+                    }
+#pragma unroll
+                for (int g = 0; g < NG; ++g)
+                    if (g == gbest) load[g] += w;
+                nkeep[si] = (unsigned char)(nk | (gbest << KEEP_BITS));
+            }
+        }
+        __syncwarp();
         mbar_arrive(S.bar_screened + 8 * b);
     }
 }
@@ -563,11 +600,10 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
     return tile;
 }
 
-// Atoms of a job go round-robin to the generation groups in the order of the
-// job's shells; the group owning an atom keeps its r^2 and coordinates.
+// The generation group evaluating a shell keeps the r^2 and coordinates of the
+// shell's atom for the following shells of the same atom.
 struct AtomRunBase {
-    int last_atom = -1, ord = -1;
-    bool mine = false;
+    int last_atom = -1;
 };
 template <int P>
 struct AtomRun : AtomRunBase {
@@ -628,7 +664,6 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
                                           uint32_t& seq, AtomRun<P>& ar, unsigned chmask, const GenPts<P>& gp,
                                           int* status)
 {
-    constexpr int NG = NTG * P / 128;  // generation groups
     const int tid = threadIdx.x;
     const int r0 = P * (tid % (128 / P));  // first point row of this thread
     const int grp = tid / (128 / P);
@@ -640,25 +675,21 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
     for (int si = ck.x; si < ck.y; ++si) {
         const Shell sh = nx;
         if (si + 1 < ck.y) nx = load_shell(B.shells + si + 1);
+        const int kb = nkeep[si];
+        const int nk = kb & MAX_PRIM;
+        if (nk == 0 || (kb >> KEEP_BITS) != grp) continue;
         if (sh.atom != ar.last_atom) {
             ar.last_atom = sh.atom;
-            ++ar.ord;
-            ar.mine = ar.ord % NG == grp;
-            if (ar.mine) {
-                const double ax = B.atoms[4 * sh.atom], ay = B.atoms[4 * sh.atom + 1], az = B.atoms[4 * sh.atom + 2];
+            const double ax = B.atoms[4 * sh.atom], ay = B.atoms[4 * sh.atom + 1], az = B.atoms[4 * sh.atom + 2];
 #pragma unroll
-                for (int i = 0; i < P; ++i) {
-                    const double X = gp.x[i] - ax, Y = gp.y[i] - ay, Z = gp.z[i] - az;
-                    ar.rr[i] = X * X + Y * Y + Z * Z;
-                    ar.X[i] = dbl_to_flt_rn(X);
-                    ar.Y[i] = dbl_to_flt_rn(Y);
-                    ar.Z[i] = dbl_to_flt_rn(Z);
-                }
+            for (int i = 0; i < P; ++i) {
+                const double X = gp.x[i] - ax, Y = gp.y[i] - ay, Z = gp.z[i] - az;
+                ar.rr[i] = X * X + Y * Y + Z * Z;
+                ar.X[i] = dbl_to_flt_rn(X);
+                ar.Y[i] = dbl_to_flt_rn(Y);
+                ar.Z[i] = dbl_to_flt_rn(Z);
             }
         }
-        if (!ar.mine) continue;
-        const int nk = nkeep[si];
-        if (nk == 0) continue;
         if constexpr (P == 1) {
             // primitives two at a time (two independent exponentials in flight)
             float R0 = 0.f, R1 = 0.f;
@@ -1201,7 +1232,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_kernel(const __
     else if (threadIdx.x < NTG + 32)
         mma_role<false>(S, P.status);
     else
-        tile_role<false>(F, S, P.status);
+        tile_role<NTG * PP / 128, false>(F, S, P.status);
     cta_teardown(S, tm_cols);
 }
 
@@ -1235,7 +1266,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(co
     else if (threadIdx.x < NTG + 32)
         mma_role<true>(S, P.status);
     else
-        tile_role<true>(F, S, P.status);
+        tile_role<NTG * PP / 128, true>(F, S, P.status);
     cta_teardown(S, 512);
 }
 
@@ -1387,6 +1418,8 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     if (major != 10 || minor != 3) return set_error(OKG_ERR_DEVICE, "okg_mixed_plan_create: needs an sm_103 GPU");
     if (b->dev.nshell > mx::MAX_SHELLS || b->dev.nmchunk > mx::MAX_CHUNKS)
         return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: more than 2048 shells or 256 column chunks");
+    if (b->dev.max_nprim > mx::MAX_PRIM)
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: a shell with more than 31 primitives");
     okg_mixed_plan* p = (okg_mixed_plan*)calloc(1, sizeof(okg_mixed_plan));
     if (!p) return set_error(OKG_ERR_ALLOC, "okg_mixed_plan_create: host allocation");
     p->basis = b;
@@ -1728,6 +1761,8 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     const size_t st_off = occ_off + (((size_t)4 * npass * npad * 8 + 255) & ~(size_t)255);
     if (b->dev.nshell > MAX_SHELLS || b->dev.nmchunk > MAX_CHUNKS)
         return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: more than 2048 shells or 256 column chunks");
+    if (b->dev.max_nprim > MAX_PRIM)
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: a shell with more than 31 primitives");
     if (st_off + 256 > NOALLOC_SCRATCH_BYTES)
         return set_error(OKG_ERR_UNSUPPORTED,
                          "okg_rho_mixed_noalloc: this basis and MO count need more than the 2 MiB of static "
