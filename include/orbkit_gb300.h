@@ -130,7 +130,7 @@ int okg_rho(const okg_basis* basis, const okg_grid* grid, int nmo, const double*
 typedef struct okg_mixed_plan okg_mixed_plan;
 /* Allocates the plan's device buffer (split coefficients, occupations, status word).
  * OKG_ERR_UNSUPPORTED for bases beyond the kernel's shared-memory tables: more than
- * 2048 shells, 256 column chunks or 31 primitives in a shell (the FP64 path has no
+ * 2048 shells, 192 column chunks or 31 primitives in a shell (the FP64 path has no
  * such limits). */
 int okg_mixed_plan_create(const okg_basis* basis, int nmo, okg_mixed_plan** out);
 /* Same with the MMA's N tile (MO columns per pass over the AO chunks) limited to

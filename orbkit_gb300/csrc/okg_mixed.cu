@@ -305,20 +305,25 @@ struct CtaState {
     uint32_t bar_bload;          // NSTAGE mbarriers: the stage's B block has landed (bulk copy)
     uint32_t bar_acc_full;       // accumulators of a job (tile, MO pass) complete (tcgen05.commit)
     uint32_t bar_acc_empty;      // every generation thread has read the accumulators
-    uint32_t bar_screened;       // 2 mbarriers (tile buffers): tile index and screening tables written
-    uint32_t bar_kfree;          // 2 mbarriers: generation threads and MMA warp are done with the buffer's tile
+    uint32_t bar_screened;       // NBUF mbarriers (tile buffers): tile index and screening tables written
+    uint32_t bar_kfree;          // NBUF mbarriers: generation threads and MMA warp are done with the buffer's tile
     uint32_t tmem;
     int* abort_flag;
-    unsigned char* nkeep;        // 2 x MAX_SHELLS: per shell, kept primitives | owning generation group << 5
-    unsigned* kmask;             // 2 x MAX_CHUNKS: per chunk, columns whose shell is kept for the buffer's tile
-    long long* tile_slot;        // 2: tile of the buffer (local to its molecule); -1: no more tiles
-    MolDesc* mol;                // 2: molecule of the buffer's tile (one copy for the single-molecule kernel)
+    unsigned char* nkeep;        // NBUF x MAX_SHELLS: per shell, kept primitives | owning generation group << 5
+    unsigned* kmask;             // NBUF x MAX_CHUNKS: per chunk, columns whose shell is kept for the buffer's tile
+    long long* tile_slot;        // NBUF: tile of the buffer (local to its molecule); -1: no more tiles
+    MolDesc* mol;                // NBUF: molecule of the buffer's tile (one copy for the single-molecule kernel)
 };
 
 // Per-tile screening tables live in shared memory: at most MAX_SHELLS shells and
 // MAX_CHUNKS chunks per molecule on the mixed path.
 constexpr int MAX_SHELLS = 2048;
-constexpr int MAX_CHUNKS = 256;
+constexpr int MAX_CHUNKS = 192;
+// Tile buffers (index, descriptor, screening tables) between the tile warp and the
+// generation threads / MMA warp: the tile warp screens up to NBUF - 1 tiles ahead.
+constexpr int NBUF = 3;
+__device__ __forceinline__ int tbuf(uint32_t ord) { return (int)(ord % NBUF); }
+__device__ __forceinline__ uint32_t tphase(uint32_t ord) { return (ord / NBUF) & 1u; }
 // A shell's byte of the screening table: kept primitives (low 5 bits, so at most
 // MAX_PRIM per shell on the mixed path) and the generation group that evaluates
 // the shell for this tile (high 3 bits, at most 8 groups).
@@ -448,8 +453,8 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
     const int lane = threadIdx.x & 31;
     long long gnext = 0, gend = 0, gpend = -1;
     for (uint32_t ord = 0;; ++ord) {
-        const int b = ord & 1;
-        if (ord >= 2 && !mbar_wait(S.bar_kfree + 8 * b, ((ord >> 1) - 1) & 1u, status)) *S.abort_flag = 1;
+        const int b = tbuf(ord);
+        if (ord >= NBUF && !mbar_wait(S.bar_kfree + 8 * b, tphase(ord - NBUF), status)) *S.abort_flag = 1;
         long long t = -1;
         int mol = 0;
         // the counter increment for the following tile (or range) is issued one
@@ -538,23 +543,37 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
             if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
         }
         __syncwarp();
-        // generation groups: per kept chunk, each kept shell goes to the group with the
-        // least estimated work so far (kept primitives and components), so every group
-        // finishes the chunk at about the same time -- the stage's "full" barrier waits
-        // for all of them.  A group recomputes an atom's coordinates only when its
-        // previous shell belonged to another atom.
+        // generation groups: per kept chunk, the kept shells in order of decreasing
+        // estimated work (kept primitives and components) each go to the group with the
+        // least work so far (longest-processing-time-first), so every group finishes the
+        // chunk at about the same time -- the stage's "full" barrier waits for all of
+        // them.  A group recomputes an atom's coordinates when its previous shell
+        // belonged to another atom.
         const int wcomp = D.want_grad ? 16 : 5;
         for (int c = lane; c < B.nmchunk; c += 32) {
             if (km[c] == 0u) continue;
             const int4 ck = B.mchunks[c];
-            int load[NG];
-#pragma unroll
-            for (int g = 0; g < NG; ++g) load[g] = 0;
-#pragma unroll 4
+            // (work << 16 | shell offset) of the kept shells, sorted descending
+            unsigned item[KC];
+            int n = 0;
             for (int si = ck.x; si < ck.y; ++si) {
                 const int nk = nkeep[si];
                 if (nk == 0) continue;
-                const int w = 3 * nk + wcomp * ncanon(B.shells[si].L);
+                const unsigned w = (unsigned)(3 * nk + wcomp * ncanon(B.shells[si].L));
+                unsigned v = (w << 16) | (unsigned)(si - ck.x);
+                int j = n++;
+                while (j > 0 && item[j - 1] < v) {
+                    item[j] = item[j - 1];
+                    --j;
+                }
+                item[j] = v;
+            }
+            int load[NG];
+#pragma unroll
+            for (int g = 0; g < NG; ++g) load[g] = 0;
+            for (int i = 0; i < n; ++i) {
+                const int si = ck.x + (int)(item[i] & 0xFFFFu);
+                const int w = (int)(item[i] >> 16);
                 int gbest = 0, lbest = load[0];
 #pragma unroll
                 for (int g = 1; g < NG; ++g)
@@ -565,7 +584,7 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
 #pragma unroll
                 for (int g = 0; g < NG; ++g)
                     if (g == gbest) load[g] += w;
-                nkeep[si] = (unsigned char)(nk | (gbest << KEEP_BITS));
+                nkeep[si] = (unsigned char)(nkeep[si] | (gbest << KEEP_BITS));
             }
         }
         __syncwarp();
@@ -582,8 +601,8 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
                                                    GenPts<P>& gp, int* status)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int b = ord & 1;
-    if (!mbar_wait(S.bar_screened + 8 * b, (ord >> 1) & 1u, status)) {
+    const int b = tbuf(ord);
+    if (!mbar_wait(S.bar_screened + 8 * b, tphase(ord), status)) {
         *S.abort_flag = 1;
         return -1;
     }
@@ -840,12 +859,12 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
     int nch = 0, nks = 0;  // chunks and K-steps issued in the current job
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     for (;;) {
-        const MolDesc& Dg = S.mol[BATCH ? (ord & 1) : 0];
-        const unsigned* km = S.kmask + (ord & 1) * MAX_CHUNKS;
+        const MolDesc& Dg = S.mol[BATCH ? tbuf(ord) : 0];
+        const unsigned* km = S.kmask + tbuf(ord) * MAX_CHUNKS;
         {
             const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
             const BasisDev& B = Dg.B;
-            const unsigned char* nkeep = S.nkeep + (ord & 1) * MAX_SHELLS;
+            const unsigned char* nkeep = S.nkeep + tbuf(ord) * MAX_SHELLS;
             while (c >= 0) {
                 gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
                 ++nch;
@@ -857,7 +876,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
         // chunk, so the buffer is released now and the tile warp screens ahead
         // during this job's epilogue (a batch releases after the stores: the buffer
         // also holds the molecule's descriptor)
-        if (!BATCH && gpass == Dg.npass - 1) mbar_arrive(S.bar_kfree + 8 * (ord & 1));
+        if (!BATCH && gpass == Dg.npass - 1) mbar_arrive(S.bar_kfree + 8 * tbuf(ord));
         // the next job: the next MO pass of this tile, or pass 0 of a new tile
         int npass_next = gpass + 1;
         uint32_t ord_next = ord;
@@ -870,12 +889,12 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
         }
         int c_next = -1, nch_next = 0, nks_next = 0;
         if (more) {
-            const MolDesc& Dn = S.mol[BATCH ? (ord_next & 1) : 0];
-            const unsigned* kmn = S.kmask + (ord_next & 1) * MAX_CHUNKS;
+            const MolDesc& Dn = S.mol[BATCH ? tbuf(ord_next) : 0];
+            const unsigned* kmn = S.kmask + tbuf(ord_next) * MAX_CHUNKS;
             ar = AtomRun<P>();
             c_next = next_kept(kmn, Dn.B.nmchunk, -1);
             if (c_next >= 0) {
-                gen_chunk<NTG, P>(Dn.B, S.nkeep + (ord_next & 1) * MAX_SHELLS, c_next, S, seq, ar,
+                gen_chunk<NTG, P>(Dn.B, S.nkeep + tbuf(ord_next) * MAX_SHELLS, c_next, S, seq, ar,
                                   Dn.want_grad ? 0xFu : 0x1u, gp, status);
                 ++nch_next;
                 nks_next += ksteps_of(kmn[c_next]);
@@ -896,7 +915,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
 #pragma unroll
             for (int o = 0; o < 4; ++o) acc[o] = 0.0;
             // this thread is done with the tile's buffer (descriptor, screening tables)
-            if (BATCH) mbar_arrive(S.bar_kfree + 8 * (ord & 1));
+            if (BATCH) mbar_arrive(S.bar_kfree + 8 * tbuf(ord));
         }
         if (!more) break;
         gpass = npass_next;
@@ -921,7 +940,7 @@ struct MmaItem {
 // MMA warp: the next kept chunk after `it` inside its tile, in (pass, chunk) order.
 __device__ __forceinline__ bool mma_next_in_tile(const CtaState& S, MmaItem& it)
 {
-    const unsigned* km = S.kmask + (it.ord & 1) * MAX_CHUNKS;
+    const unsigned* km = S.kmask + tbuf(it.ord) * MAX_CHUNKS;
     for (;;) {
         ++it.c;
         if (it.c == it.nmchunk) {
@@ -947,12 +966,12 @@ __device__ __forceinline__ bool mma_open_next(const CtaState& S, MmaItem& it, bo
     for (;;) {
         if (release) {
             __syncwarp();
-            if (lane == 0) mbar_arrive(S.bar_kfree + 8 * (it.ord & 1));
+            if (lane == 0) mbar_arrive(S.bar_kfree + 8 * tbuf(it.ord));
             ++it.ord;
         }
         release = true;
-        const int b = it.ord & 1;
-        if (!mbar_wait(S.bar_screened + 8 * b, (it.ord >> 1) & 1u, status)) *S.abort_flag = 1;
+        const int b = tbuf(it.ord);
+        if (!mbar_wait(S.bar_screened + 8 * b, tphase(it.ord), status)) *S.abort_flag = 1;
         if (S.tile_slot[b] < 0 || *S.abort_flag) return false;
         const MolDesc& D = S.mol[BATCH ? b : 0];
         it.bpack = D.bpack;
@@ -1106,10 +1125,10 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
     S.A_s = smem;
     S.B_s = smem + NSTAGE * A_STAGE;
     S.kmask = (unsigned*)(S.B_s + NSTAGE * B_STAGE);
-    // full[2], empty[2], bload[2], acc full, acc empty, screened[2], kfree[2]
-    uint64_t* bar = (uint64_t*)(S.kmask + 2 * MAX_CHUNKS);
-    S.tile_slot = (long long*)(bar + 12);
-    uint32_t* tmem_slot = (uint32_t*)(S.tile_slot + 2);
+    // full[2], empty[2], bload[2], acc full, acc empty, screened[NBUF], kfree[NBUF]
+    uint64_t* bar = (uint64_t*)(S.kmask + NBUF * MAX_CHUNKS);
+    S.tile_slot = (long long*)(bar + 8 + 2 * NBUF);
+    uint32_t* tmem_slot = (uint32_t*)(S.tile_slot + NBUF);
     S.abort_flag = (int*)(tmem_slot + 1);
     S.nkeep = (unsigned char*)(S.abort_flag + 1);
     S.mol = mol;
@@ -1119,7 +1138,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
     S.bar_acc_full = smem_u32(bar + 6);
     S.bar_acc_empty = smem_u32(bar + 7);
     S.bar_screened = smem_u32(bar + 8);
-    S.bar_kfree = smem_u32(bar + 10);
+    S.bar_kfree = smem_u32(bar + 8 + NBUF);
     for (int i = tid; i < NSTAGE * A_STAGE / 16; i += NTT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
@@ -1129,7 +1148,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
         }
         mbar_init(S.bar_acc_full, 1);
         mbar_init(S.bar_acc_empty, NTG);
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NBUF; ++b) {
             mbar_init(S.bar_screened + 8 * b, 32);     // the tile warp
             mbar_init(S.bar_kfree + 8 * b, NTG + 1);   // every generation thread and the MMA warp
         }
@@ -1150,9 +1169,9 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
 }
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
-constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * 2 * MAX_CHUNKS + 12 * 8 + 2 * 8 + 4 + 4 +
-                              2 * MAX_SHELLS + 64;
-static_assert(SMEM_BYTES + 2 * sizeof(MolDesc) <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
+constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * NBUF * MAX_CHUNKS + (8 + 2 * NBUF) * 8 +
+                              NBUF * 8 + 4 + 4 + NBUF * MAX_SHELLS + 64;
+static_assert(SMEM_BYTES + NBUF * sizeof(MolDesc) <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 static_assert(KC == 32, "column masks are 32-bit and operand rows one 64-byte swizzle row");
 static_assert(sizeof(MolDesc) % 16 == 0, "descriptors are copied in 16-byte units");
 
@@ -1252,7 +1271,7 @@ struct BatchParams {
 template <int NTG, int PP>
 __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(const BatchParams P)
 {
-    __shared__ MolDesc mol[2];
+    __shared__ MolDesc mol[NBUF];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
     CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, 512);
     TileFeed F;
@@ -1417,7 +1436,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (major != 10 || minor != 3) return set_error(OKG_ERR_DEVICE, "okg_mixed_plan_create: needs an sm_103 GPU");
     if (b->dev.nshell > mx::MAX_SHELLS || b->dev.nmchunk > mx::MAX_CHUNKS)
-        return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: more than 2048 shells or 256 column chunks");
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: more than 2048 shells or 192 column chunks");
     if (b->dev.max_nprim > mx::MAX_PRIM)
         return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: a shell with more than 31 primitives");
     okg_mixed_plan* p = (okg_mixed_plan*)calloc(1, sizeof(okg_mixed_plan));
@@ -1760,7 +1779,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     const size_t occ_off = (bpack_bytes + 255) & ~(size_t)255;
     const size_t st_off = occ_off + (((size_t)4 * npass * npad * 8 + 255) & ~(size_t)255);
     if (b->dev.nshell > MAX_SHELLS || b->dev.nmchunk > MAX_CHUNKS)
-        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: more than 2048 shells or 256 column chunks");
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: more than 2048 shells or 192 column chunks");
     if (b->dev.max_nprim > MAX_PRIM)
         return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed_noalloc: a shell with more than 31 primitives");
     if (st_off + 256 > NOALLOC_SCRATCH_BYTES)
