@@ -27,10 +27,11 @@
 // (<= 64 per pass), K = canonical Cartesian AO columns in chunks of 32 (one
 // 64-byte swizzle row of BF16).  Persistent CTAs, one per SM, each with
 // 128 x NG generation threads (NG threads per grid point), one MMA warp and one
-// tile warp.  The tile warp takes tiles from a device counter and screens them up
-// to two tiles ahead (double-buffered tile index, descriptor and screening tables,
-// handed over through "screened" and "kfree" mbarriers).  Generation threads and
-// the MMA warp are connected by a two-stage ring in shared memory:
+// tile warp.  The tile warp takes tiles from a device counter, screens them and
+// assigns their shells to the generation groups, up to two tiles ahead (three
+// buffers of tile index, descriptor and screening tables, handed over through
+// "screened" and "kfree" mbarriers).  Generation threads and the MMA warp are
+// connected by a two-stage ring in shared memory:
 //   * generation threads write 4 channels x 3 parts of A (128 x 32 BF16, K-major,
 //     SWIZZLE_64B) for a chunk into a free stage and arrive on its "full" barrier;
 //   * the MMA warp bulk-copies the chunk's pre-split, pre-swizzled B block into the
@@ -441,11 +442,12 @@ struct GenPts {
 };
 
 // Tile warp (the last warp of the CTA): takes tiles from the feed into buffer
-// ord % 2 once the generation threads and the MMA warp have released that buffer's
-// previous tile, computes the tile's bounding box and screens every shell against
-// it (primitives kept per shell, kept columns per chunk), then arrives on the
-// buffer's "screened" barrier.  It runs up to two tiles ahead of the generation
-// threads, so none of this is on their path.  A buffer with tile -1 ends the CTA.
+// ord % NBUF once the generation threads and the MMA warp have released that
+// buffer's previous tile, computes the tile's bounding box, screens every shell
+// against it (primitives kept per shell, kept columns per chunk) and assigns the
+// kept shells to generation groups, then arrives on the buffer's "screened"
+// barrier.  It runs up to NBUF - 1 tiles ahead of the generation threads, so none
+// of this is on their path.  A buffer with tile -1 ends the CTA.
 template <int NG, bool BATCH>
 __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, int* status)
 {
