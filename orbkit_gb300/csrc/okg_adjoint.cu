@@ -35,6 +35,10 @@ constexpr int NT = P * NW;
 constexpr int MB = 6;
 constexpr int NMOMAX = NW * MB;
 constexpr int KC = OKG_KC;
+// Persistent CTAs: two per SM in FP32 (at most 128 registers per thread, 72 KB of
+// shared memory each), one in FP64.
+template <typename T>
+__host__ __device__ constexpr int ctas_per_sm() { return sizeof(T) == 4 ? 2 : 1; }
 
 template <typename T>
 struct Args {
@@ -131,7 +135,7 @@ __device__ __forceinline__ void shell_sums_L(int L, T X, T Y, T Z, T gx, T gy, T
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT, 1) adjoint_kernel(BasisDev B, Grid g, Args<T> A)
+__global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev B, Grid g, Args<T> A)
 {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     T* AO_s = (T*)sm_raw;            // 10 x KC x P
@@ -339,13 +343,15 @@ size_t workspace_bytes(const okg_basis* b, int nmo, int nblk)
     return (size_t)nblk * ((size_t)nmo * b->ncart + 2 * (size_t)b->nprim + (size_t)NW * b->natom * 3) * sizeof(T) + 256;
 }
 
+template <typename T>
 static int block_count(long long ntiles)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
-    return (int)(ntiles < sms ? (ntiles > 0 ? ntiles : 1) : sms);
+    const long long cap = (long long)sms * ctas_per_sm<T>();
+    return (int)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
 }
 
 template <typename T>
@@ -354,7 +360,7 @@ static int run(const okg_basis* b, const Grid& g, int nmo, const double* C, cons
                size_t work_bytes, cudaStream_t st)
 {
     const long long ntiles = (g.npts + P - 1) / P;
-    const int nblk = block_count(ntiles);
+    const int nblk = block_count<T>(ntiles);
     if (work_bytes < workspace_bytes<T>(b, nmo, nblk))
         return set_error(OKG_ERR_ARG, "okg_rho_backward: workspace smaller than okg_rho_backward_workspace reports");
     Args<T> A;
@@ -395,8 +401,8 @@ extern "C" int okg_rho_backward_workspace(const okg_basis* b, const okg_grid* gr
 {
     if (!b || !grid || !bytes || nmo <= 0) return set_error(OKG_ERR_ARG, "okg_rho_backward_workspace: bad argument");
     const long long ntiles = (grid->npts + adj::P - 1) / adj::P;
-    const int nblk = adj::block_count(ntiles);
-    *bytes = precision == 32 ? adj::workspace_bytes<float>(b, nmo, nblk) : adj::workspace_bytes<double>(b, nmo, nblk);
+    *bytes = precision == 32 ? adj::workspace_bytes<float>(b, nmo, adj::block_count<float>(ntiles))
+                             : adj::workspace_bytes<double>(b, nmo, adj::block_count<double>(ntiles));
     return OKG_OK;
 }
 
