@@ -214,3 +214,56 @@ def test_gaussian_cube_golden():
                          ("rho_valence", val, 1e-5), ("homo", mo, 1e-5)):
         cube_close(a, d["cube_" + name], tol)
         _same(a, d["ref_" + name], name)
+
+
+def test_detci_matrix_folding_matches_term_sums():
+    """Host side of the detCI quadratic forms (orbkit_gb300.detci.density_matrix /
+    flux_matrix and the matrices handed to okg_ci_rho_matrix / okg_ci_flux_matrix),
+    evaluated with numpy as the kernels define them, against the oracle's term-order
+    sums of orbkit's loops: the three state pairs of the H3+ test on seeded MO grids."""
+    from helpers import detci_terms
+    from orbkit_gb300 import detci
+    d = numpy.load(GOLDEN + "/h3p_detci.npz")
+    rng = numpy.random.default_rng(3)
+    nmo = 42
+    mo = rng.standard_normal((nmo, 300))
+    dr = rng.standard_normal((3, nmo, 300))
+    for k in range(int(d["npairs"])):
+        zero, sing = detci_terms(d, k)
+        M = detci.density_matrix(zero, sing, nmo)
+        S = M + M.T
+        S[numpy.diag_indices(nmo)] = numpy.diag(M)
+        qt = numpy.tril(S)  # row b: coefficients of MO_a, a <= b
+        rho = numpy.einsum("bp,ba,ap->p", mo, qt, mo)
+        r0 = okref.ci_rho(zero, sing, mo)
+        assert numpy.abs(rho - r0).max() <= 1e-12 * numpy.abs(r0).max()
+        C = detci.flux_matrix(sing, nmo)
+        for Q, scale, fn in ((C - C.T, -0.5, okref.ci_jab), (C, 1.0, okref.ci_a_nabla_b)):
+            j = scale * numpy.einsum("dbp,ba,ap->dp", dr, Q.T, mo)
+            j0 = fn(zero, sing, mo, dr)
+            assert numpy.abs(j - j0).max() <= 1e-12 * numpy.abs(j0).max()
+    # index checks happen on the host
+    with pytest.raises(IndexError):
+        detci.density_matrix([[[1.0]], [[nmo]]], [[], []], nmo)
+
+
+def test_atom2mo_and_lc_match_reference(ref):
+    """get_atom2mo / get_lc of orbkit_gb300.analytical_integrals against the reference's
+    (orbkit/analytical_integrals.py:442-505) for Cartesian and spherical fixtures."""
+    from orbkit import analytical_integrals as ai_ref
+    from orbkit_gb300 import analytical_integrals as ai
+    from refpkg import to_reference_qc
+    from orbkit.tools import exp, lquant
+    for name in ("small_cart.npz", "h2o_molden.npz", "sph_fg_N.npz"):
+        qc, _ = load_golden(name)
+        q = to_reference_qc(ref, qc)
+        for s in q.ao_spec:
+            if "lxlylz" in s and [tuple(r) for r in s["lxlylz"]] == list(exp[lquant[s["type"]]]):
+                del s["lxlylz"]
+        q.ao_spec.update()
+        a_ref = ai_ref.get_atom2mo(q)
+        numpy.testing.assert_array_equal(ai.get_atom2mo(qc), a_ref)
+        for atoms in (0, [0, 2], [1]):
+            numpy.testing.assert_array_equal(ai.get_lc(atoms, a_ref), ai_ref.get_lc(atoms, a_ref))
+            numpy.testing.assert_array_equal(ai.get_lc(atoms, a_ref, strict=True),
+                                             ai_ref.get_lc(atoms, a_ref, strict=True))
