@@ -81,3 +81,16 @@ def cube_case():
 def cube_close(a, b, tol):
     """The reference's test/tools.py equal(): allclose(a, b, rtol=100 tol, atol=tol)."""
     numpy.testing.assert_allclose(a, b, rtol=tol * 1e2, atol=tol)
+
+
+def analytic_cases():
+    """The cases of h2o_analytic.npz: (name, qc, dict of the case's arrays)."""
+    d = numpy.load(os.path.join(GOLDEN, "h2o_analytic.npz"), allow_pickle=False)
+    out = []
+    for k, name in enumerate(d["names"]):
+        pre = "c%d__" % k
+        arrs = {key[len(pre):]: d[key] for key in d.files if key.startswith(pre)}
+        qc = from_arrays(arrs)
+        qc.geo_info = [["X", str(i + 1), repr(float(z))] for i, z in enumerate(arrs["charges"])]
+        out.append((str(name), qc, arrs))
+    return out

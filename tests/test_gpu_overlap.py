@@ -110,3 +110,28 @@ def test_argument_errors(ai):
         ai.get_ao_overlap(geo[:1], geo, qc.ao_spec)
     with pytest.raises(TypeError):
         ai.get_ao_overlap(geo, geo, list(qc.ao_spec))
+
+
+def test_analytic_property_kats(ai):
+    """The reference's analytic-property tests on the GPU path (test/analytical_properties/
+    analytical_integral_norm.py, dipole.py; tests/golden/h2o_analytic.npz): H2O RHF/UHF,
+    Cartesian/spherical, read from molden, Gaussian log/fchk and aomix files -- AO and MO
+    overlaps and dipole moments against the reference's values (FP64 bar), MOs orthonormal
+    and dipoles equal to the quantum-chemistry programs' own values (those tests' tolerances)."""
+    from helpers import analytic_cases, cube_close
+    for name, qc, a in analytic_cases():
+        geo = numpy.asarray(qc.geo_spec)
+        S = ai.get_ao_overlap(geo, geo, qc.ao_spec)
+        assert_fp64_close(S, a["aoom"], name + " AO overlap")
+        C = qc.mo_spec.get_coeffs()
+        for spin in ("alpha", "beta"):
+            idx = a["idx_" + spin]
+            if len(idx) == 0:
+                continue
+            moom = ai.get_mo_overlap_matrix(C[idx], C[idx], S)
+            assert_fp64_close(moom, a["moom_" + spin], name + " MO overlap " + spin)
+            if not name.endswith("moved"):  # moving one atom leaves the MOs non-orthogonal
+                cube_close(moom, numpy.eye(len(idx)), 1e-4)
+        dip = ai.get_dipole_moment(qc)
+        assert numpy.abs(dip - a["dipole"]).max() <= 1e-12 * max(1.0, numpy.abs(a["dipole"]).max()), name
+        cube_close(dip, a["kat_dip"], 1e-5)

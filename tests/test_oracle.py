@@ -267,3 +267,29 @@ def test_atom2mo_and_lc_match_reference(ref):
             numpy.testing.assert_array_equal(ai.get_lc(atoms, a_ref), ai_ref.get_lc(atoms, a_ref))
             numpy.testing.assert_array_equal(ai.get_lc(atoms, a_ref, strict=True),
                                              ai_ref.get_lc(atoms, a_ref, strict=True))
+
+
+def test_analytic_integral_kats():
+    """The reference's analytic-property tests (test/analytical_properties/
+    analytical_integral_norm.py, dipole.py): H2O RHF/UHF, Cartesian/spherical, from
+    molden, Gaussian log/fchk and aomix files.  The oracle reproduces the reference's AO
+    overlap, MO overlap matrices and dipole moments (tests/golden/h2o_analytic.npz), the MOs
+    are orthonormal and the dipoles match the quantum-chemistry programs' own values,
+    with the tolerances of those tests."""
+    from helpers import analytic_cases
+    for name, qc, a in analytic_cases():
+        geo = qc.geo_spec
+        S = okref.ao_overlap(geo, geo, qc.ao_spec)
+        _same(S, a["aoom"], name + " AO overlap")
+        C = qc.mo_spec.get_coeffs()
+        for spin in ("alpha", "beta"):
+            idx = a["idx_" + spin]
+            if len(idx) == 0:
+                continue
+            moom = okref.mo_overlap_matrix(C[idx], C[idx], S)
+            _same(moom, a["moom_" + spin], name + " MO overlap " + spin)
+            if not name.endswith("moved"):  # moving one atom leaves the MOs non-orthogonal
+                cube_close(moom, numpy.eye(len(idx)), 1e-4)
+        dip = okref.dipole_moment(qc, a["charges"])
+        _same(dip, a["dipole"], name + " dipole")
+        cube_close(dip, a["kat_dip"], 1e-5)
