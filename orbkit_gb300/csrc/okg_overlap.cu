@@ -38,6 +38,7 @@
 #include "okg_internal.cuh"
 
 #define OKG_OV_MAXV 24  // longest vertical recursion: max l_bra + max l_ket + 2
+#define OV_PAIR_TABLE_MAX (2ull << 30)  // bytes of the primitive-pair table a plan may hold
 
 namespace okg {
 
@@ -73,17 +74,65 @@ __device__ __forceinline__ void os_axis(double xpa, double ab, double p, int la,
     sp = v[la];
 }
 
+// Quantities of a primitive pair (bra primitive i at its atom in geo_a, ket primitive j
+// at its atom in geo_b) shared by every Cartesian component pair of the two shells:
+// p = alpha + beta, pref = exp(-mu R^2) (pi/p)^(3/2) (0 where the exponential
+// underflows) and P - A per axis.  Evaluated once per call into a table of
+// nprim x nprim entries when the plan holds one, with the same operations as the
+// element kernel's own evaluation.
+struct alignas(16) OvPair {
+    double pref, p, xpa[3], pad;
+};
+
+__global__ void ov_pairs_kernel(int nprim, const double2* __restrict__ prim, const int* __restrict__ prim_atom,
+                                const double* __restrict__ geo_a, const double* __restrict__ geo_b,
+                                OvPair* __restrict__ pairs)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= nprim || j >= nprim) return;
+    const double al = prim[i].x, be = prim[j].x;
+    double A[3], B[3];
+    double rr = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        A[d] = geo_a[3 * prim_atom[i] + d];
+        B[d] = geo_b[3 * prim_atom[j] + d];
+        const double ab = A[d] - B[d];
+        rr = fma(ab, ab, rr);
+    }
+    OvPair e;
+    const double inv_p = 1.0 / (al + be);
+    const double arg = al * be * inv_p * rr;
+    e.p = al + be;
+    if (arg > 746.0) {
+        e.pref = 0.0;  // exp(-arg) is 0 in double
+    } else {
+        const double t = M_PI * inv_p;
+        e.pref = exp(-arg) * t * sqrt(t);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double P = __dadd_rn(__dmul_rn(al, A[d]), __dmul_rn(be, B[d])) / e.p;
+        e.xpa[d] = -(A[d] - P);
+    }
+    e.pad = 0.0;
+    pairs[(long long)i * nprim + j] = e;
+}
+
 // A warp computes 32 elements of one bra row I.  Its kets are consecutive in the
 // plan's ket order (sorted by primitive count, then exponents), so the lanes run
 // the same primitive loops and recursion lengths; a primitive pair is skipped only
 // when exp(-mu R^2) underflows for every lane (it contributes exactly 0 to the
 // others as well).
+template <bool TABLE>
 __global__ void __launch_bounds__(256) ao_overlap_kernel(int nrow, const OvRow* __restrict__ rows,
                                                          const int* __restrict__ ket_order,
                                                          const double2* __restrict__ prim,
                                                          const double* __restrict__ pnorm,
                                                          const double* __restrict__ geo_a,
-                                                         const double* __restrict__ geo_b, int drv,
+                                                         const double* __restrict__ geo_b,
+                                                         const OvPair* __restrict__ pairs, int nprim, int drv,
                                                          double* __restrict__ out, long long ld)
 {
     const int Jo = blockIdx.x * blockDim.x + threadIdx.x;
@@ -110,21 +159,39 @@ __global__ void __launch_bounds__(256) ao_overlap_kernel(int nrow, const OvRow* 
             const double2 pb = prim[rj.prim0 + jp];
             const double nb = pnorm[rj.rp0 + jp];
             const double al = pa.x, be = pb.x;
-            const double inv_p = 1.0 / (al + be);
-            const double arg = al * be * inv_p * rr;
-            if (__all_sync(__activemask(), arg > 746.0)) continue;  // exp(-arg) is 0 in double: adds exactly 0
-            const double eab = exp(-arg);
-            const double t = M_PI * inv_p;
-            const double pref = eab * t * sqrt(t);
-            const double p = al + be;
+            double pref, p, xpa_t[3];
+            if (TABLE) {
+                const double2* e = reinterpret_cast<const double2*>(pairs + (long long)(ri.prim0 + ip) * nprim +
+                                                                   rj.prim0 + jp);
+                const double2 e0 = e[0], e1 = e[1], e2 = e[2];
+                pref = e0.x;
+                p = e0.y;
+                xpa_t[0] = e1.x;
+                xpa_t[1] = e1.y;
+                xpa_t[2] = e2.x;
+                if (__all_sync(__activemask(), pref == 0.0)) continue;  // the pair adds exactly 0
+            } else {
+                const double inv_p = 1.0 / (al + be);
+                const double arg = al * be * inv_p * rr;
+                if (__all_sync(__activemask(), arg > 746.0)) continue;  // exp(-arg) is 0 in double: adds exactly 0
+                const double eab = exp(-arg);
+                const double t = M_PI * inv_p;
+                pref = eab * t * sqrt(t);
+                p = al + be;
+            }
             // product of the 1D factors of the non-derivative axes, in axis order;
             // along the derivative axis the two shifted factors are kept apart
             double s_plain = pref, s_minus = pref, s_plus = pref;
             int lbd = 0;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const double P = __dadd_rn(__dmul_rn(al, A[d]), __dmul_rn(be, B[d])) / p;
-                const double xpa = -(A[d] - P);
+                double xpa;
+                if (TABLE) {
+                    xpa = xpa_t[d];
+                } else {
+                    const double P = __dadd_rn(__dmul_rn(al, A[d]), __dmul_rn(be, B[d])) / p;
+                    xpa = -(A[d] - P);
+                }
                 const int la = lcomp(ri.la, d), lb = lcomp(rj.lb, d);
                 const bool deriv = (d == dd);
                 double s0, sm, sp;
@@ -187,6 +254,8 @@ using namespace okg;
 
 struct okg_overlap_plan {
     int* ket_order = nullptr;  // kets sorted by (primitive count, exponents): the kernel's column order
+    int* prim_atom = nullptr;  // atom of every primitive
+    OvPair* pairs = nullptr;   // nprim x nprim primitive-pair table (NULL above OV_PAIR_TABLE_MAX bytes)
     int natom, nshell, ncart, nprim, nout;
     int max_la;
     int spherical, has_renorm;
@@ -241,6 +310,8 @@ static void ov_free(okg_overlap_plan* p)
     cudaFree(p->tcoef);
     cudaFree(p->work);
     cudaFree(p->ket_order);
+    cudaFree(p->prim_atom);
+    cudaFree(p->pairs);
     delete p;
 }
 
@@ -363,6 +434,23 @@ extern "C" int okg_overlap_plan_create(int natom, int nshell, const int* h_shell
         ov_free(P);
         return cuda_status(e, "okg_overlap_plan_create: workspace");
     }
+    // primitive-pair table (geometry-dependent, filled by every okg_ao_overlap call)
+    const size_t pair_bytes = (size_t)nprim * nprim * sizeof(OvPair);
+    if (pair_bytes <= OV_PAIR_TABLE_MAX) {
+        std::vector<int> prim_atom;
+        prim_atom.reserve(nprim);
+        for (int sh = 0; sh < nshell; ++sh)
+            for (int q = 0; q < h_shell_nprim[sh]; ++q) prim_atom.push_back(h_shell_atom[sh]);
+        if ((st = ov_upload(&P->prim_atom, prim_atom.data(), prim_atom.size(), "okg_overlap_plan_create"))) {
+            ov_free(P);
+            return st;
+        }
+        e = cudaMalloc((void**)&P->pairs, pair_bytes);
+        if (e != cudaSuccess) {
+            ov_free(P);
+            return cuda_status(e, "okg_overlap_plan_create: primitive-pair table");
+        }
+    }
     *out = P;
     return OKG_OK;
 }
@@ -423,8 +511,16 @@ extern "C" int okg_ao_overlap(okg_overlap_plan* plan, const double* d_geo_a, con
     const long long lds = direct ? ld : plan->ncart;
     const dim3 blk(32, 8);
     const dim3 grd((plan->ncart + 31) / 32, (plan->ncart + 7) / 8);
-    ao_overlap_kernel<<<grd, blk, 0, st>>>(plan->ncart, plan->rows, plan->ket_order, plan->prim, plan->pnorm, d_geo_a,
-                                          d_geo_b, drv, S, lds);
+    if (plan->pairs) {
+        const dim3 gpp((plan->nprim + 31) / 32, (plan->nprim + 7) / 8);
+        ov_pairs_kernel<<<gpp, blk, 0, st>>>(plan->nprim, plan->prim, plan->prim_atom, d_geo_a, d_geo_b, plan->pairs);
+        ao_overlap_kernel<true><<<grd, blk, 0, st>>>(plan->ncart, plan->rows, plan->ket_order, plan->prim,
+                                                    plan->pnorm, d_geo_a, d_geo_b, plan->pairs, plan->nprim, drv,
+                                                    S, lds);
+    } else {
+        ao_overlap_kernel<false><<<grd, blk, 0, st>>>(plan->ncart, plan->rows, plan->ket_order, plan->prim,
+                                                     plan->pnorm, d_geo_a, d_geo_b, nullptr, 0, drv, S, lds);
+    }
     int s = cuda_status(cudaGetLastError(), "okg_ao_overlap launch");
     if (s || direct) return s;
     const dim3 tblk(16, 16);
