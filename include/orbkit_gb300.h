@@ -254,7 +254,10 @@ int okg_ci_flux_matrix(int64_t npts, const double* d_mo, const double* d_drv, in
  * The plan takes the arrays of okg_basis_create plus the primitives (h_prim,
  * nprim x 2 [alpha, c]; ao_spec.get_prim_coeffs()) on the host; per (listed row,
  * primitive) norms ao_norm (orbkit/c_support.c:177-188) are computed once from the
- * bra exponents h_lxlylz, as orbkit does for both bra and ket. */
+ * bra exponents h_lxlylz, as orbkit does for both bra and ket.  The plan allocates its
+ * device tables, an ncart x ncart workspace and, when it takes at most 2 GiB, an
+ * nprim x nprim x 48-byte table of primitive-pair quantities that every okg_ao_overlap
+ * call refills for its geometries. */
 typedef struct okg_overlap_plan okg_overlap_plan;
 int okg_overlap_plan_create(int natom, int nshell, const int* h_shell_atom, const int* h_shell_ncart,
                             const int* h_shell_nprim, const int* h_lxlylz, int is_normalized, const double* h_prim,

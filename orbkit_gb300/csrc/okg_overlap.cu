@@ -4,7 +4,9 @@
 // (orbkit/analytical_integrals.py:37-116) over cy_overlap.aooverlap
 // (orbkit/cy_overlap.pyx:78-163) and get_overlap (orbkit/c_non-grid-based.c:9-52).
 //
-// One thread per output Cartesian pair (I, J).  It walks the primitives of I (outer)
+// Per call, a table holds what a primitive pair shares across all component pairs of
+// its two shells (p, the prefactor, P - A; ov_pairs_kernel).  Then one thread per
+// output Cartesian pair (I, J).  It walks the primitives of I (outer)
 // and of J (inner), which is the order orbkit's flattened primitive loop adds them
 // to aoom[I, J].  The 1D factors are evaluated with orbkit's operations and
 // rounding (IEEE divisions, no FMA contraction): the two terms of a derivative can
