@@ -22,7 +22,6 @@ reference extension itself (tests/test_oracle.py).
 import ctypes
 import os
 import subprocess
-import sysconfig
 
 import numpy
 
