@@ -13,31 +13,53 @@ from .orbitals import AOClass, MOClass  # noqa: F401
 from .qcinfo import QCinfo  # noqa: F401
 
 
-def install(orbkit_module):
-    """Route orbkit.core's grid functions to this package.
+# orbkit submodule -> (module of this package, functions replaced)
+ROUTES = [
+    ("core", "core", ["ao_creator", "mo_creator", "cartesian2spherical", "rho_compute", "rho_compute_no_slice",
+                      "calc_mo_matrix"]),
+    ("extras", "extras", ["calc_jmo"]),
+    ("detci.ci_core", "detci", ["rho", "jab", "a_nabla_b"]),
+    ("analytical_integrals", "analytical_integrals",
+     ["get_ao_overlap", "cartesian2spherical_aoom", "get_mo_overlap", "get_mo_overlap_matrix", "get_moom_atoms",
+      "check_mo_norm", "get_dipole_moment", "get_ao_dipole_matrix", "get_nuclear_dipole_moment", "get_atom2mo",
+      "get_lc"]),
+]
 
-    ``orbkit_module`` is the imported orbkit package.  ao_creator, mo_creator,
-    cartesian2spherical, rho_compute, rho_compute_no_slice and calc_mo_matrix of
-    orbkit.core (and the names re-exported at the package level) are replaced;
-    they read orbkit.grid.  Returns a function that restores the originals."""
-    from . import core as ours
-    okc = orbkit_module.core
-    names = ["ao_creator", "mo_creator", "cartesian2spherical", "rho_compute", "rho_compute_no_slice",
-             "calc_mo_matrix"]
-    saved = {n: getattr(okc, n) for n in names}
-    saved_pkg = {n: getattr(orbkit_module, n) for n in names if hasattr(orbkit_module, n)}
-    saved_grid = ours.grid
-    ours.grid = orbkit_module.grid
-    for n in names:
-        setattr(okc, n, getattr(ours, n))
-        if n in saved_pkg:
-            setattr(orbkit_module, n, getattr(ours, n))
+
+def install(orbkit_module):
+    """Route orbkit's grid and analytic-integral functions to this package.
+
+    ``orbkit_module`` is the imported orbkit package.  Replaced: ao_creator,
+    mo_creator, cartesian2spherical, rho_compute, rho_compute_no_slice and
+    calc_mo_matrix of orbkit.core (they read orbkit.grid); calc_jmo of orbkit.extras;
+    rho, jab and a_nabla_b of orbkit.detci.ci_core; the overlap, MO-overlap and dipole
+    functions of orbkit.analytical_integrals -- and the same names where the package
+    re-exports them.  Submodules orbkit cannot import are left alone.  Returns a
+    function that restores the originals."""
+    import importlib
+    from . import core as ours_core
+    saved = []
+    for sub, mine, names in ROUTES:
+        try:
+            target = importlib.import_module(orbkit_module.__name__ + "." + sub)
+        except ImportError:
+            continue
+        ours = importlib.import_module(__name__ + "." + mine)
+        for n in names:
+            orig = getattr(target, n, None)
+            if orig is None:
+                continue
+            saved.append((target, n, orig))
+            setattr(target, n, getattr(ours, n))
+            if getattr(orbkit_module, n, None) is orig:  # re-exported at the package level
+                saved.append((orbkit_module, n, orig))
+                setattr(orbkit_module, n, getattr(ours, n))
+    saved_grid = ours_core.grid
+    ours_core.grid = orbkit_module.grid
 
     def restore():
-        for n, f in saved.items():
-            setattr(okc, n, f)
-        for n, f in saved_pkg.items():
-            setattr(orbkit_module, n, f)
-        ours.grid = saved_grid
+        for obj, n, f in reversed(saved):
+            setattr(obj, n, f)
+        ours_core.grid = saved_grid
 
     return restore

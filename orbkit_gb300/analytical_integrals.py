@@ -137,8 +137,8 @@ def get_ao_overlap(coord_a, coord_b, ao_spec, lxlylz_b=None, drv=None):
     (orbkit/analytical_integrals.py:37-116): lxlylz_b replaces the ket's Cartesian
     exponents (the primitive norms still use ao_spec's), drv = 'x', 'y', 'z' (or
     1..3) differentiates the ket, a list of drv returns a list of matrices."""
-    if not isinstance(ao_spec, AOClass):
-        raise TypeError('ao_spec must be an instance of the AOClass')
+    if not (isinstance(ao_spec, AOClass) or hasattr(ao_spec, "get_lxlylz")):
+        raise TypeError('ao_spec must be an instance of the AOClass')  # orbkit's own AOClass is accepted too
     if isinstance(drv, list) or (isinstance(drv, str) and len(drv) > 1):
         return [get_ao_overlap(coord_a, coord_b, ao_spec, lxlylz_b=lxlylz_b, drv=d) for d in drv]
     lxlylz_a = ao_spec.get_lxlylz()
@@ -180,7 +180,7 @@ def cartesian2spherical_aoom(ao_overlap_matrix, ao_spec):
 
 
 def _coeffs(mo):
-    if isinstance(mo, MOClass):
+    if isinstance(mo, MOClass) or hasattr(mo, "get_coeffs"):  # this package's MOClass or orbkit's
         return mo.get_coeffs()
     if isinstance(mo, dict):
         return numpy.array(mo['coeffs'])

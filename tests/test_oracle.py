@@ -293,3 +293,34 @@ def test_analytic_integral_kats():
         dip = okref.dipole_moment(qc, a["charges"])
         _same(dip, a["dipole"], name + " dipole")
         cube_close(dip, a["kat_dip"], 1e-5)
+
+
+def test_install_routes_and_restores(ref):
+    """orbkit_gb300.install swaps the reference package's grid, detCI, extras and
+    analytic-integral functions (module and package level) and restores them."""
+    import orbkit_gb300
+    from orbkit_gb300 import analytical_integrals, core, detci, extras
+    import orbkit.analytical_integrals as ai_ref
+    import orbkit.detci.ci_core as ci_ref
+    originals = {
+        (ref.core, "rho_compute"): ref.core.rho_compute,
+        (ref, "rho_compute"): ref.rho_compute,
+        (ref.extras, "calc_jmo"): ref.extras.calc_jmo,
+        (ref, "calc_jmo"): ref.calc_jmo,
+        (ci_ref, "jab"): ci_ref.jab,
+        (ai_ref, "get_ao_overlap"): ai_ref.get_ao_overlap,
+        (ai_ref, "get_dipole_moment"): ai_ref.get_dipole_moment,
+        (ref, "get_dipole_moment"): ref.get_dipole_moment,
+    }
+    restore = orbkit_gb300.install(ref)
+    try:
+        assert ref.core.rho_compute is core.rho_compute and ref.rho_compute is core.rho_compute
+        assert ref.extras.calc_jmo is extras.calc_jmo and ref.calc_jmo is extras.calc_jmo
+        assert ci_ref.rho is detci.rho and ci_ref.jab is detci.jab and ci_ref.a_nabla_b is detci.a_nabla_b
+        assert ai_ref.get_ao_overlap is analytical_integrals.get_ao_overlap
+        assert ref.get_dipole_moment is analytical_integrals.get_dipole_moment
+        assert core.grid is ref.grid
+    finally:
+        restore()
+    for (obj, name), f in originals.items():
+        assert getattr(obj, name) is f, name
