@@ -324,3 +324,61 @@ def test_install_routes_and_restores(ref):
         restore()
     for (obj, name), f in originals.items():
         assert getattr(obj, name) is f, name
+
+
+@pytest.mark.parametrize("name", ["small_cart.npz", "sph_fg_N.npz", "normalized.npz", "h2o_gaussian_cube.npz"])
+def test_oracle_vs_reference_extension_fixtures(ref, name):
+    """Bit-identical AOs (all drv codes), MOs and rho / grad rho / Laplacian against the
+    reference's compiled cy_core on the fixture molecules (Cartesian, spherical f/g with
+    'N', pre-normalised, Gaussian fchk) at seeded random points."""
+    from refpkg import to_reference_qc as ref_qc
+    qc, _ = load_golden(name)
+    q = ref_qc(ref, qc)
+    rng = numpy.random.default_rng(len(name))
+    x, y, z = rng.uniform(-4, 4, (3, 257))
+    for dv in DRV_ALL:
+        a = ref.core.ao_creator(q.geo_spec, q.ao_spec, drv=dv, x=x, y=y, z=z, is_vector=True)
+        b = okref.ao_creator(qc.geo_spec, qc.ao_spec, drv=dv, x=x, y=y, z=z)
+        _same(b, a, "%s ao drv=%s" % (name, dv))
+    R = ref.core.rho_compute_no_slice(q, drv=["x", "y", "z", "xx", "yz"], laplacian=True, x=x, y=y, z=z,
+                                      is_vector=True)
+    O = okref.rho_compute_no_slice(qc, drv=["x", "y", "z", "xx", "yz"], laplacian=True, x=x, y=y, z=z)
+    for k in range(len(R)):
+        _same(O[k], R[k], "%s rho_compute_no_slice output %d" % (name, k))
+
+
+def test_detci_oracle_vs_reference_extension(ref):
+    """The oracle's detCI loops against the reference's compiled cy_ci (get_rho, get_jab,
+    get_a_nabla_b) on the H3+ terms with seeded MO grids: bit for bit."""
+    from helpers import detci_terms
+    from orbkit.detci import cy_ci
+    d = numpy.load(GOLDEN + "/h3p_detci.npz")
+    rng = numpy.random.default_rng(9)
+    mo = numpy.ascontiguousarray(rng.standard_normal((42, 211)))
+    dr = numpy.ascontiguousarray(rng.standard_normal((3, 42, 211)))
+    for k in range(int(d["npairs"])):
+        zero, sing = detci_terms(d, k)
+        _same(okref.ci_rho(zero, sing, mo), cy_ci.get_rho(0, 211, zero, sing, mo), "rho %d" % k)
+        _same(okref.ci_jab(zero, sing, mo, dr), cy_ci.get_jab(0, 211, zero, sing, mo, dr), "jab %d" % k)
+        _same(okref.ci_a_nabla_b(zero, sing, mo, dr), cy_ci.get_a_nabla_b(0, 211, zero, sing, mo, dr),
+              "a_nabla_b %d" % k)
+
+
+def test_overlap_oracle_vs_reference_extension(ref):
+    """okref_aooverlap against the reference's compiled cy_overlap.aooverlap on the
+    mid-size molecule: plain, the three ket derivatives and a second ket geometry."""
+    from orbkit import cy_overlap
+    from orbkit_gb300 import synthetic
+    qc = synthetic.mid()["qc"]
+    ao = qc.ao_spec
+    geo = numpy.ascontiguousarray(qc.geo_spec, dtype=numpy.float64)
+    geo2 = numpy.ascontiguousarray(geo + numpy.random.default_rng(1).uniform(-0.3, 0.3, geo.shape))
+    lx = numpy.ascontiguousarray(ao.get_lxlylz(), dtype=numpy.intc)
+    args = (numpy.ascontiguousarray(ao.get_nlxlylz_per_cont(), dtype=numpy.intc),
+            numpy.ascontiguousarray(ao.get_prim_coeffs(), dtype=numpy.float64),
+            numpy.ascontiguousarray(ao.get_nprim_per_cont(), dtype=numpy.intc),
+            numpy.ascontiguousarray(ao.get_assign_cont_to_atoms(), dtype=numpy.intc))
+    for gb in (geo, geo2):
+        for drv in range(4):
+            r = cy_overlap.aooverlap(geo, gb, lx, lx, *args, drv, int(ao.get_normalized()))
+            _same(okref.aooverlap(geo, gb, lx, lx, ao, drv), r, "aooverlap drv=%d" % drv)
