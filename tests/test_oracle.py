@@ -382,3 +382,22 @@ def test_overlap_oracle_vs_reference_extension(ref):
         for drv in range(4):
             r = cy_overlap.aooverlap(geo, gb, lx, lx, *args, drv, int(ao.get_normalized()))
             _same(okref.aooverlap(geo, gb, lx, lx, ao, drv), r, "aooverlap drv=%d" % drv)
+
+
+def test_argument_errors_match_reference(ref):
+    """Invalid derivative selectors and mismatched grid vectors raise the reference's
+    exception types and messages, before any device work (orbkit/tools.py:225-239,
+    orbkit/core.py:79-80)."""
+    from orbkit_gb300 import core
+    from refpkg import to_reference_qc
+    qc, _ = load_golden("small_cart.npz")
+    q = to_reference_qc(ref, qc)
+    x = numpy.linspace(-1, 1, 3)
+    cases = [dict(drv="q", x=x, y=x, z=x), dict(drv=11, x=x, y=x, z=x), dict(drv=None, x=x, y=x[:2], z=x)]
+    for kw in cases:
+        with pytest.raises(Exception) as e_ref:
+            ref.core.ao_creator(q.geo_spec, q.ao_spec, is_vector=True, **kw)
+        with pytest.raises(Exception) as e_ours:
+            core.ao_creator(qc.geo_spec, qc.ao_spec, is_vector=True, **kw)
+        assert type(e_ours.value) is type(e_ref.value), kw
+        assert str(e_ours.value) == str(e_ref.value), kw
