@@ -401,3 +401,24 @@ def test_argument_errors_match_reference(ref):
             core.ao_creator(qc.geo_spec, qc.ao_spec, is_vector=True, **kw)
         assert type(e_ours.value) is type(e_ref.value), kw
         assert str(e_ours.value) == str(e_ref.value), kw
+
+
+def test_overlap_argument_errors_match_reference(ref):
+    """get_ao_overlap's argument checks raise the reference's exceptions and messages
+    before any device work (orbkit/analytical_integrals.py:66-97)."""
+    from orbkit import analytical_integrals as ai_ref
+    from orbkit_gb300 import analytical_integrals as ai
+    from refpkg import to_reference_qc
+    qc, _ = load_golden("small_cart.npz")
+    q = to_reference_qc(ref, qc)
+    geo = numpy.asarray(qc.geo_spec)
+    cases = [dict(drv=4), dict(lxlylz_b=numpy.zeros((3, 3), dtype=int)), dict(drv="q")]
+    for kw in cases:
+        with pytest.raises(Exception) as e_ref:
+            ai_ref.get_ao_overlap(geo, geo, q.ao_spec, **kw)
+        with pytest.raises(Exception) as e_ours:
+            ai.get_ao_overlap(geo, geo, qc.ao_spec, **kw)
+        assert type(e_ours.value) is type(e_ref.value), kw
+        assert str(e_ours.value) == str(e_ref.value), kw
+    with pytest.raises(TypeError):
+        ai.get_ao_overlap(geo, geo, list(qc.ao_spec))
