@@ -523,7 +523,7 @@ def run_workload(args):
         rel = [float((g32 - g64).abs().max() / g64.abs().max()) for g32, g64 in zip(res["fp32"][2], res["fp64"][2])]
         npts = res["fp64"][1]
         out.update({"metric": "grid points/s for loss + gradient (dL/dC, dL/dalpha, dL/dc, dL/dR), FP32 vs FP64",
-                    "value": npts / (res["fp32"][0] * 1e-3), "ms_per_step": res["fp32"][0],
+                    "value": npts / (res["fp32"][0] * 1e-3), "ms_per_step": res["fp32"][0], "dtype": "f32",
                     "config": {"workload": "grad: 12 atoms, 128^3 grid, density-fitting loss, forward + adjoint",
                                "npts": npts, "fp64": {"value": npts / (res["fp64"][0] * 1e-3),
                                                       "ms_per_step": res["fp64"][0]},

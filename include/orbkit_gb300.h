@@ -148,7 +148,9 @@ int okg_mixed_plan_set_threads(okg_mixed_plan* plan, int threads);
 int okg_mixed_plan_set_generation(okg_mixed_plan* plan, int threads, int points_per_thread);
 /* Split C_eff (nmo x ncart, FP64, device) into the BF16 operand tiles; copy occ (nmo). */
 int okg_mixed_set_coeffs(okg_mixed_plan* plan, const double* d_coeff, const double* d_occ, okg_stream stream);
-/* d_rho[i]; d_grad[c * ld + i] for c = x, y, z when want_grad. */
+/* d_rho[i]; d_grad[c * ld + i] for c = x, y, z when want_grad.  Every point is
+ * evaluated by the tensor-core kernel, the cusp region near nuclei included: the
+ * Python layer (orbkit_gb300.mixed) recomputes the points near nuclei with okg_rho. */
 int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, double* d_rho, double* d_grad,
                   int64_t ld, okg_stream stream);
 /* Synchronising check of the plan's device status word (bounded tensor-core waits):
@@ -202,9 +204,13 @@ int okg_rho_backward(const okg_basis* basis, const okg_grid* grid, int nmo, cons
  * d_coeff (C_eff, nmo x ncart) and occupations d_occ are split into a 2 MiB
  * file-scope device array on every call instead of a plan's buffer; larger
  * (basis, nmo) combinations return OKG_ERR_UNSUPPORTED.  The first call on a device
- * looks up the array and sets up the kernel (make it before any stream capture).
- * Calls that overlap on the GPU race on the shared array.  A tensor-core wait that
- * expires sets *d_status to 1 (d_status may be NULL; the call clears it first). */
+ * looks up the array and sets up the kernel (make it before any stream capture);
+ * the looked-up address is kept for the process, so do not use this entry point
+ * across a cudaDeviceReset.  Calls that overlap on the GPU race on the shared array.
+ * d_status (required, a device int) is cleared by the call and set to 1 by the
+ * kernel if a tensor-core wait expired (the outputs are then incomplete).  As with
+ * okg_rho_mixed, every point -- the cusp region near nuclei included -- comes from
+ * the tensor-core kernel (no FP64 recomputation at this level). */
 int okg_rho_mixed_noalloc(const okg_basis* basis, const okg_grid* grid, int nmo, const double* d_coeff,
                           const double* d_occ, int want_grad, double* d_rho, double* d_grad, int64_t ld,
                           int* d_status, okg_stream stream);

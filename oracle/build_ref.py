@@ -29,7 +29,10 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
+# the reference tree: $ORBKIT_REFERENCE_ROOT, else a checkout named "reference"
+# beside this repository
+DEFAULT_REF = os.environ.get("ORBKIT_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 
 # (module name, [pyx], [extra C sources]) -- mirrors setup.py:51-75 of the reference
 EXTENSIONS = [

@@ -18,7 +18,10 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("ORBKIT_REFERENCE_ROOT", "/root/reference")
+# the reference tree: $ORBKIT_REFERENCE_ROOT, else a checkout named "reference"
+# beside this repository
+REF_ROOT = os.environ.get("ORBKIT_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference")
 
 
 def _stub(name):

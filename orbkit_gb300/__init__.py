@@ -34,7 +34,8 @@ def install(orbkit_module):
     calc_mo_matrix of orbkit.core (they read orbkit.grid); calc_jmo of orbkit.extras;
     rho, jab and a_nabla_b of orbkit.detci.ci_core; the overlap, MO-overlap and dipole
     functions of orbkit.analytical_integrals -- and the same names where the package
-    re-exports them.  Submodules orbkit cannot import are left alone.  Returns a
+    re-exports them.  Submodules orbkit cannot import are left alone.  Terminal
+    output (MO norms, electron count) then goes through orbkit's display.  Returns a
     function that restores the originals."""
     import importlib
     from . import core as ours_core
@@ -56,10 +57,16 @@ def install(orbkit_module):
                 setattr(orbkit_module, n, getattr(ours, n))
     saved_grid = ours_core.grid
     ours_core.grid = orbkit_module.grid
+    saved_display = ours_core.display
+    try:
+        ours_core.display = importlib.import_module(orbkit_module.__name__ + ".display").display
+    except (ImportError, AttributeError):
+        pass
 
     def restore():
         for obj, n, f in reversed(saved):
             setattr(obj, n, f)
         ours_core.grid = saved_grid
+        ours_core.display = saved_display
 
     return restore

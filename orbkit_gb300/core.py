@@ -31,6 +31,35 @@ grid = _default_grid
 # points per device slice (bounded so that slice outputs stay a few GB)
 MAX_SLICE_BYTES = 4 << 30
 
+# orbkit's terminal output (orbkit/display.py: display); install() routes it to
+# orbkit's own display, which honours orbkit.options.quiet and the .oklog file
+quiet = False
+
+
+def display(msg):
+    if not quiet:
+        print(msg)
+
+
+def _report(rho, mo_norm, mo_spec, d3r, was_vector, drv, calc_ao=False):
+    """The MO norms (regular grid, no derivatives) and the electron count (regular
+    grid) that orbkit's rho_compute prints (orbkit/core.py:572-592)."""
+    if was_vector:
+        return
+    if drv is None and mo_norm is not None:
+        display("\nNorm of the MOs:")
+        labels = mo_spec.get_labels(format="print")
+        for i in range(len(mo_norm)):
+            display("\t%(m).6f\t%(t)s %(n)s" % {"m": mo_norm[i] * d3r, "n": labels[i], "t": "AO" if calc_ao else "MO"})
+    display("We have " + str(numpy.sum(rho) * d3r) + " electrons.")
+
+
+def _report_norms_no_slice(norms, mo_spec, d3r):
+    """The MO norms rho_compute_no_slice prints (orbkit/core.py:797-802)."""
+    display("\nNorm of the MOs:")
+    for i in range(len(norms)):
+        display("\t%(m).6f\tMO %(n)s" % {"m": norms[i] * d3r, "n": mo_spec[i].get("sym", "?")})
+
 
 def _torch():
     import torch
@@ -112,9 +141,11 @@ def _drv_list(drv):
         return [drv]
 
 
-def _eval(qc_geo, ao_spec, mo_spec, x, y, z, is_vector, what, drv_codes, exact_mixed=False, occ=None):
+def _eval(qc_geo, ao_spec, mo_spec, x, y, z, is_vector, what, drv_codes, exact_mixed=False, occ=None,
+          mo_norm=False):
     """Evaluate on the GPU.  what: 'ao' -> (ndrv, nao, npts); 'mo' -> (ndrv, nmo, npts);
-    'rho' -> (rho (npts,), drho (ndrv, npts))."""
+    'rho' -> (rho (npts,), drho (ndrv, npts)), plus the MO norms sum_i MO_m(i)^2
+    (nmo,) when mo_norm is true."""
     torch = _torch()
     L = _lib.load()
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -150,6 +181,7 @@ def _eval(qc_geo, ao_spec, mo_spec, x, y, z, is_vector, what, drv_codes, exact_m
     if occ is None:
         occ = numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64)
     occ_d = torch.as_tensor(numpy.asarray(occ, dtype=numpy.float64), device=dev).contiguous()
+    norm_d = torch.zeros(nmo, dtype=torch.float64, device=dev) if mo_norm else None
     rho = numpy.empty(npts)
     drho = numpy.empty((nd, npts))
     for (i, j) in _slices(npts, 8 * (1 + nd)):
@@ -159,10 +191,12 @@ def _eval(qc_geo, ao_spec, mo_spec, x, y, z, is_vector, what, drv_codes, exact_m
         r = torch.empty(j - i, dtype=torch.float64, device=dev)
         dr = torch.empty((max(nd, 1), j - i), dtype=torch.float64, device=dev)
         _lib.check(L.okg_rho(b.handle, gd, nmo, _lib.ptr(C), _lib.ptr(occ_d), nd, codes, em, _lib.ptr(r),
-                             _lib.ptr(dr), j - i, None, st))
+                             _lib.ptr(dr), j - i, _lib.ptr(norm_d), st))
         rho[i:j] = r.cpu().numpy()
         if nd:
             drho[:, i:j] = dr[:nd].cpu().numpy()
+    if mo_norm:
+        return rho, drho, norm_d.cpu().numpy()
     return rho, drho
 
 
@@ -248,7 +282,10 @@ def rho_compute(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, num
     vec = grid.is_vector
     x, y, z, vec, N = _grid_arrays(grid.x, grid.y, grid.z, vec, use_module=False)
     if precision == "mixed" and _mixed_ok(calc_mo, drv, laplacian):
-        return _mixed_rho(qc, x, y, z, vec, N, drv)
+        out = _mixed_rho(qc, x, y, z, vec, N, drv)
+        # (the tensor-core kernel forms no MO norms: only the electron count is reported)
+        _report(out if drv is None else out[0], None, mo_spec, grid.d3r, vec, drv)
+        return out
     codes = [0] if drv is None else [validate_drv(d) for d in drv]
     if calc_mo:
         what = "ao" if calc_ao else "mo"
@@ -258,7 +295,10 @@ def rho_compute(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=False, num
             return out.reshape((out.shape[0],) + N)
         return out.reshape(out.shape[:2] + N)
     rcodes = [] if drv is None else codes
-    rho, drho = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed)
+    want_norm = drv is None and not vec
+    res = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed, mo_norm=want_norm)
+    rho, drho = res[0], res[1]
+    _report(rho, res[2] if want_norm else None, mo_spec, grid.d3r, vec, drv)
     rho = rho.reshape(N)
     if drv is None:
         return rho
@@ -294,10 +334,21 @@ def rho_compute_no_slice(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=F
     if calc_ao:
         return ao_list
     mo_list = conv(_eval(geo, ao_spec, mo_spec, x, y, z, vec, "mo", [0])[0]) if (calc_mo or return_components) else None
+    d3r = 1.0
+    for v in (x, y, z):
+        if len(v) > 1:
+            d3r *= v[1] - v[0]
+    if mo_list is not None and not vec:
+        _report_norms_no_slice(numpy.array([numpy.sum(m ** 2) for m in mo_list]), mo_spec, d3r)
     if calc_mo:
         return (ao_list, mo_list) if return_components else mo_list
     rcodes = [] if drv is None else codes
-    rho, drho = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed)
+    res = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed, mo_norm=mo_list is None and not vec)
+    rho, drho = res[0], res[1]
+    if not vec:
+        if mo_list is None:
+            _report_norms_no_slice(res[2], mo_spec, d3r)
+        display("We have " + str(numpy.sum(rho) * d3r) + " electrons.")
     rho = conv(rho)
     if drv is None:
         return (ao_list, mo_list, rho) if return_components else rho

@@ -1726,11 +1726,19 @@ extern "C" int okg_mixed_status(okg_mixed_plan* p, int* device_status)
 //   that loads the library holds the array until the process exits.
 // * The first call on a device looks up the array's device address
 //   (cudaGetSymbolAddress) and sets the kernel's shared-memory attribute, with that
-//   device current; make that first call before any stream capture.
+//   device current; make that first call before any stream capture.  The address
+//   is kept for the life of the process: do not use the entry point across a
+//   cudaDeviceReset (which invalidates it).
+// * The caller passes a device int for the timeout status (required): the call
+//   clears it on the stream and the kernel sets it to 1 if a tensor-core wait
+//   expired, in which case the outputs are incomplete.
 // * All calls on a device share the one array and it keeps the last call's
 //   contents: calls that overlap on the GPU (different streams, or host threads
 //   that do not order their streams) race on it.  Each call rewrites every byte it
-//   reads and clears the status word before its kernels run.
+//   reads and clears the tile counter before its kernels run.
+// * Like okg_rho_mixed, it evaluates every point on the tensor cores: the points
+//   near nuclei are not recomputed in FP64 (the Python layer does that for the
+//   plan path).
 // ---------------------------------------------------------------------------
 #include <mutex>
 
@@ -1757,6 +1765,9 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     using namespace okg::mx;
     if (!b || !gr || !d_coeff || !d_occ || !d_rho || (want_grad && !d_grad) || nmo <= 0)
         return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: NULL argument or nmo <= 0");
+    // the timeout status goes to the caller's word: a word inside the shared scratch
+    // could not be read back, and an expired wait would go unnoticed
+    if (!d_status) return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: d_status is NULL");
     Grid g;
     g.x = gr->d_x;
     g.y = gr->d_y;
@@ -1773,7 +1784,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
         return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: regular grid range outside Nx*Ny*Nz");
     if (ld < g.npts) return set_error(OKG_ERR_ARG, "okg_rho_mixed_noalloc: ld < npts");
 
-    // scratch layout: split coefficients | occupations | status word
+    // scratch layout: split coefficients | occupations | tile counter
     const int npass = (nmo + NMAX - 1) / NMAX;
     const int per = (nmo + npass - 1) / npass;
     const int npad = (per + 15) / 16 * 16;
@@ -1816,7 +1827,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     cudaStream_t st = (cudaStream_t)stream;
     __nv_bfloat16* bpack = (__nv_bfloat16*)nd->base;
     double* occ = (double*)(nd->base + occ_off);
-    int* status = d_status ? d_status : (int*)(nd->base + st_off);
+    int* status = d_status;
     e = cudaMemsetAsync(status, 0, sizeof(int), st);
     if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: clear status");
     const BasisDev& B = b->dev;
