@@ -369,6 +369,10 @@ def run_profile(args):
         return _profile_detci()
     if args.workload == "overlap":
         return _profile_overlap()
+    if args.workload == "large":
+        return _profile_large()
+    if args.workload == "ao":
+        return _profile_ao()
     import torch
     from orbkit_gb300 import _lib, mixed, synthetic
     from orbkit_gb300.core import _DeviceGrid
@@ -392,6 +396,62 @@ def run_profile(args):
     torch.cuda.synchronize()
     ev.check()
     print("profile run done: %d points" % npts)
+
+
+def _profile_large():
+    """The large basis (2420 Cartesian AOs, 400 MOs) on a 128 x 128 x 64 block of its
+    grid (2^20 points, brick tiles) on the mixed path, and the FP64 fused kernel on
+    2^16 of those points; each twice."""
+    import torch
+    from orbkit_gb300 import _lib, mixed, synthetic
+    from orbkit_gb300.core import _DeviceGrid
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    L = _lib.load()
+    w = synthetic.large()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    bx, by, bz = gx[64:192], gy[64:192], gz[96:160]
+    ev = mixed.MixedEvaluator(qc, device=dev, cusp_radius=0.0)
+    g = _DeviceGrid(bx, by, bz, False, dev)
+    n = g.npts
+    gd, keep = g.slice(0, n)
+    rho = torch.empty(n, dtype=torch.float64, device=dev)
+    grad = torch.empty((3, n), dtype=torch.float64, device=dev)
+    n64 = 1 << 16
+    gd64, keep64 = g.slice(n // 2, n // 2 + n64)
+    codes = _lib.int_array([1, 2, 3])
+    for _ in range(2):
+        ev.plan.rho(gd, rho, grad, n)
+        _lib.check(L.okg_rho(ev.basis.handle, gd64, ev.plan.nmo, _lib.ptr(ev.plan.C), _lib.ptr(ev.plan.occ), 3, codes,
+                             0, _lib.ptr(rho), _lib.ptr(grad), n64, None, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    ev.check()
+    print("profile run done: large, %d points mixed, %d FP64" % (n, n64))
+
+
+def _profile_ao():
+    """okg_eval_ao (drv 0) on the mid molecule: 40 x 160 x 160 points of its grid
+    (1 024 000 points, 180 AOs: 1.47 GB written), twice."""
+    import torch
+    from orbkit_gb300 import _lib, synthetic
+    from orbkit_gb300.basis import get_basis
+    from orbkit_gb300.core import _DeviceGrid
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    L = _lib.load()
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    b = get_basis(qc.geo_spec, qc.ao_spec, dev)
+    g = _DeviceGrid(gx[60:100], gy, gz, False, dev)
+    n = g.npts
+    gd, keep = g.slice(0, n)
+    out = torch.empty((b.nao, n), dtype=torch.float64, device=dev)
+    for _ in range(2):
+        _lib.check(L.okg_eval_ao(b.handle, gd, 1, _lib.int_array([0]), 0, _lib.ptr(out), n, _lib.stream_handle()))
+    torch.cuda.synchronize()
+    print("profile run done: ao, %d points x %d AOs" % (n, b.nao))
 
 
 def _profile_detci():
@@ -462,38 +522,7 @@ def run_workload(args):
     out = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic", "dtype": "bf16"}
     if name in ("small", "large"):
-        w = synthetic.small() if name == "small" else synthetic.large()
-        qc = w["qc"]
-        gx, gy, gz = w["grid"]
-        npts = len(gx) * len(gy) * len(gz)
-        ev = mixed.MixedEvaluator(qc, device=dev)
-        g = _DeviceGrid(gx, gy, gz, False, dev)
-        rho = torch.empty(npts, dtype=torch.float64, device=dev)
-        grad = torch.empty((3, npts), dtype=torch.float64, device=dev)
-        ms = _time_ms(lambda: ev.evaluate_device(g, rho, grad), args.steps, args.warmup, flush)
-        ev.check()
-        # FP64 path: whole grid (small) or a contiguous slice of 2^18 points (large)
-        n64 = npts if name == "small" else 1 << 18
-        gd, keep = g.slice(npts // 2, npts // 2 + n64) if n64 < npts else g.slice(0, npts)
-        r64 = torch.empty(n64, dtype=torch.float64, device=dev)
-        g64 = torch.empty((3, n64), dtype=torch.float64, device=dev)
-        p = ev.plan
-        fp64_ms = _time_ms(lambda: _lib.check(L.okg_rho(ev.basis.handle, gd, p.nmo, _lib.ptr(p.C), _lib.ptr(p.occ),
-                                                        3, _lib.int_array([1, 2, 3]), 0, _lib.ptr(r64),
-                                                        _lib.ptr(g64), n64, None, _lib.stream_handle())), 1, 1)
-        s0 = npts // 2 if n64 < npts else 0
-        err = mixed.error_report(rho[s0:s0 + n64].cpu().numpy(), grad[:, s0:s0 + n64].cpu().numpy(),
-                                 r64.cpu().numpy(), g64.cpu().numpy())
-        out.update({"value": npts / (ms * 1e-3), "ms_per_step": ms,
-                    "config": {"workload": name, "npts": npts, "nao": ev.basis.nao, "ncart": ev.basis.ncart,
-                               "nmo": p.nmo, "spherical": ev.basis.spherical, "path": "mixed",
-                               "fp64_path": {"value": n64 / (fp64_ms * 1e-3), "points_timed": n64},
-                               "mixed_over_fp64": (n64 / fp64_ms) and (npts / ms) / (n64 / fp64_ms),
-                               "max_rel_err": dict(err, against="FP64 GPU path on the %d points it timed" % n64)}})
-        if not args.no_cpu_baseline:
-            rate, cores, n, dt = cpu_rate(qc, gx, gy, gz, target_s=8.0)
-            out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                                   "sample": "%d random grid points, %.1f s" % (n, dt)}
+        out.update(_single_workload(args, name, flush, L))
     elif name == "grad":
         from orbkit_gb300.adjoint import DensityModel, density_fit_loss
         w = synthetic.grad()
@@ -551,11 +580,124 @@ def run_workload(args):
                                "launch": "CUDA graph replay of one persistent kernel", "cusp_radius": 0.0,
                                "with_fp64_cusp_points": {"cusp_radius": mixed.CUSP_RADIUS, "cusp_points": ncusp,
                                                          "value": npts / (ms1 * 1e-3), "ms_per_step": ms1}}})
+    elif name == "ao":
+        out.update(_ao_workload(args, flush, L))
     elif name == "overlap":
         out.update(_overlap_workload(args, flush))
     elif name == "detci":
         out.update(_detci_workload(args, flush))
     print(json.dumps(out))
+
+
+def _single_workload(args, name, flush, L):
+    """The small or large molecule on its full regular grid: mixed path (value), its
+    kernel alone (tensor roofline), and the FP64 path on a seeded random sample of the
+    grid's points (whole grid for small; 2^18 points for large) with its FP64-pipe
+    roofline; the mixed path's error against the FP64 path at those points."""
+    import torch
+    from orbkit_gb300 import _lib, mixed, synthetic
+    from orbkit_gb300.core import _DeviceGrid
+    dev = torch.device("cuda", 0)
+    w = synthetic.small() if name == "small" else synthetic.large()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    npts = len(gx) * len(gy) * len(gz)
+    ev = mixed.MixedEvaluator(qc, device=dev)
+    b, p = ev.basis, ev.plan
+    g = _DeviceGrid(gx, gy, gz, False, dev)
+    gd, keep = g.slice(0, npts)
+    rho = torch.empty(npts, dtype=torch.float64, device=dev)
+    grad = torch.empty((3, npts), dtype=torch.float64, device=dev)
+    ms = _time_ms(lambda: ev.evaluate_device(g, rho, grad), args.steps, args.warmup, flush)
+    ev.check()
+    kms = _time_ms(lambda: p.rho(gd, rho, grad, npts), max(3, args.steps), 1, flush)
+    ev.evaluate_device(g, rho, grad)
+    # FP64 path on a seeded random sample of the grid (a vector grid of those points)
+    if name == "small":
+        idx = numpy.arange(npts)
+    else:
+        idx = numpy.sort(numpy.random.default_rng(9).choice(npts, 1 << 18, replace=False))
+    n64 = len(idx)
+    nyz = len(gy) * len(gz)
+    pts = [torch.from_numpy(numpy.ascontiguousarray(v)).to(dev)
+           for v in (gx[idx // nyz], gy[(idx // len(gz)) % len(gy)], gz[idx % len(gz)])]
+    gd64 = _lib.OkgGrid(pts[0].data_ptr(), pts[1].data_ptr(), pts[2].data_ptr(), n64, 0, 0, 0, 0, 0)
+    r64 = torch.empty(n64, dtype=torch.float64, device=dev)
+    g64 = torch.empty((3, n64), dtype=torch.float64, device=dev)
+    codes = _lib.int_array([1, 2, 3])
+    fp64_ms = _time_ms(lambda: _lib.check(L.okg_rho(b.handle, gd64, p.nmo, _lib.ptr(p.C), _lib.ptr(p.occ), 3, codes,
+                                                    0, _lib.ptr(r64), _lib.ptr(g64), n64, None,
+                                                    _lib.stream_handle())), 2, 1, flush)
+    it = torch.from_numpy(idx).to(dev)
+    err = mixed.error_report(rho[it].cpu().numpy(), grad[:, it].cpu().numpy(), r64.cpu().numpy(), g64.cpu().numpy())
+    pk, pk_kind = peaks()
+    tflops = 8.0 * p.nmo * b.nao * npts / (kms * 1e-3) / 1e12
+    fma64 = 4.0 * p.nmo * b.ncart * n64 / (fp64_ms * 1e-3)
+    fpk = fp64_fma_peak()
+    res = {"value": npts / (ms * 1e-3), "ms_per_step": ms,
+           "config": {"workload": name, "npts": npts, "nao": b.nao, "ncart": b.ncart, "nmo": p.nmo,
+                      "spherical": b.spherical, "path": "mixed",
+                      "fp64_path": {"value": n64 / (fp64_ms * 1e-3), "points_timed": n64,
+                                    "sample": "all grid points" if n64 == npts else
+                                    "seeded random sample of the grid's points (vector grid)"},
+                      "mixed_over_fp64": (npts / ms) / (n64 / fp64_ms),
+                      "max_rel_err": dict(err, against="FP64 GPU path at the %d points it timed" % n64)},
+           "roofline": {"bound": "tensor", "achieved": tflops, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                        "frac": tflops / pk["bf16_tflops"], "traffic": profile_traffic("rho_mixed_kernel_" + name),
+                        "kernel": "rho_mixed_kernel", "kernel_ms": kms,
+                        "peak_source": "bf16 burst, %s (MEASURED_PEAKS.json)" % pk_kind,
+                        "algorithmic": "8*NMO*NAO FLOP per point (value + 3 derivatives of C.AO)",
+                        "fp64_path": {"bound": "fp64", "achieved": fma64, "peak": fpk, "unit": "FMA/s",
+                                      "frac": fma64 / fpk, "kernel": "fused64_kernel", "kernel_ms": fp64_ms,
+                                      "traffic": profile_traffic("fused64_kernel_" + name),
+                                      "algorithmic": "4*NMO*NCART FMA per point (C.AO for value + 3 derivatives)",
+                                      "peak_source": "2 DFMA/clk/SM x SMs x max SM clock"}},
+           "gpu_launches": args.steps * 2}
+    if not args.no_cpu_baseline:
+        rate, cores, n, dt = cpu_rate(qc, gx, gy, gz, target_s=8.0)
+        res["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "%d random grid points, %.1f s" % (n, dt)}
+    return res
+
+
+def _ao_workload(args, flush, L):
+    """AO values (drv 0, and the three first derivatives) of the mid molecule on 40 x
+    160 x 160 points of its grid through okg_eval_ao: the HBM roofline of the AO
+    kernel (8 B written per (AO, point, drv); a regular grid reads no coordinates)."""
+    import torch
+    from orbkit_gb300 import _lib, synthetic
+    from orbkit_gb300.basis import get_basis
+    from orbkit_gb300.core import _DeviceGrid
+    dev = torch.device("cuda", 0)
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    b = get_basis(qc.geo_spec, qc.ao_spec, dev)
+    g = _DeviceGrid(gx[60:100], gy, gz, False, dev)
+    n = g.npts
+    gd, keep = g.slice(0, n)
+    res = {}
+    for nd, codes in ((1, [0]), (4, [0, 1, 2, 3])):
+        out = torch.empty((nd, b.nao, n), dtype=torch.float64, device=dev)
+        ca = _lib.int_array(codes)
+        ms = _time_ms(lambda: _lib.check(L.okg_eval_ao(b.handle, gd, nd, ca, 0, _lib.ptr(out), n,
+                                                       _lib.stream_handle())), args.steps, args.warmup, flush)
+        res[nd] = (ms, 8.0 * nd * b.nao * n)
+        del out
+    pk, pk_kind = peaks()
+    ms, byt = res[1]
+    gbs = byt / (ms * 1e-3) / 1e9
+    gbs4 = res[4][1] / (res[4][0] * 1e-3) / 1e9
+    return {"metric": "AO values written per second (okg_eval_ao), GB/s", "unit": "GB/s", "value": gbs,
+            "ms_per_step": ms, "dtype": "f64",
+            "config": {"workload": "ao: mid molecule (180 Cartesian AOs), 40 x 160 x 160 = %d grid points, drv 0" % n,
+                       "with_first_derivatives": {"ndrv": 4, "ms_per_step": res[4][0], "GB/s": gbs4}},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": gbs / pk["hbm_gbs"], "traffic": profile_traffic("ao_eval_kernel"),
+                         "kernel": "ao_eval_kernel", "kernel_ms": ms,
+                         "algorithmic": "8 B written per (AO, point, drv)",
+                         "peak_source": "HBM copy, %s (MEASURED_PEAKS.json)" % pk_kind},
+            "gpu_launches": args.steps}
 
 
 def _oracle():
@@ -721,7 +863,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-step-s", type=float, default=4.0)
     ap.add_argument("--profile", action="store_true", help="minimal launch sequence for ncu captures")
-    ap.add_argument("--workload", default="mid", choices=["mid", "small", "grad", "batch", "large", "overlap", "detci"])
+    ap.add_argument("--workload", default="mid",
+                    choices=["mid", "small", "grad", "batch", "large", "overlap", "detci", "ao"])
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)

@@ -121,6 +121,37 @@ int okg_rho(const okg_basis* basis, const okg_grid* grid, int nmo, const double*
             int ndrv, const int* h_drv, int exact_mixed, double* d_rho, double* d_drho, int64_t ld,
             double* d_mo_norm, okg_stream stream);
 
+/* ------------------------------------------------ operations on given grids
+ * FP64 operations on AO / MO values the caller already holds on the device, every
+ * array row-major (row, point) with points contiguous and its own leading dimension
+ * (ld >= npts), as orbkit's ao_list[k, i] / mo_list[m, i]. */
+/* MO = C . AO: d_out[m * ld_out + i] = sum_k d_coeff[m * nao + k] d_ao[k * ld_ao + i]
+ * (FMA accumulation).  Replaces cy_core.mocreator (orbkit/cy_core.pyx:82-101) behind
+ * core.mo_creator (orbkit/core.py:107-132). */
+int okg_mo_from_ao(int nmo, int nao, const double* d_coeff, const double* d_ao, int64_t ld_ao, int64_t npts,
+                   double* d_out, int64_t ld_out, okg_stream stream);
+/* Spherical rows from Cartesian rows: d_out[r * ld_out + i] = sum over t in
+ * [d_ptr[r], d_ptr[r+1]) of d_coef[t] d_in[d_cart[t] * ld_in + i], terms added in
+ * order with one rounding per product and per sum (orbkit's numpy arithmetic, bit for
+ * bit).  d_cart entries must lie in [0, ncart) (others give NaN).  Replaces
+ * core.cartesian2spherical (orbkit/core.py:135-176); the CSR arrays are those of
+ * okg_basis_create's spherical transform (coefficient x global factor). */
+int okg_cart2sph(int nsph, int ncart, const int* d_ptr, const int* d_cart, const double* d_coef, const double* d_in,
+                 int64_t ld_in, int64_t npts, double* d_out, int64_t ld_out, okg_stream stream);
+/* MO products of calc_mo_matrix (orbkit/core.py:935-937):
+ * d_out[((d * na + n) * nb + m) * ld_out + i] = d_bra[n * ld_bra + i] * d_ket[(d * nb + m) * ld_ket + i]
+ * (one rounded multiply: orbkit's values bit for bit). */
+int okg_mo_products(int ndrv, int na, int nb, const double* d_bra, int64_t ld_bra, const double* d_ket,
+                    int64_t ld_ket, int64_t npts, double* d_out, int64_t ld_out, okg_stream stream);
+/* Transition flux densities of extras.calc_jmo (orbkit/extras.py:441-492) for MO
+ * pairs (i, j) = (d_pairs[2q], d_pairs[2q+1]) in [0, nmo) (others give NaN):
+ * d_out[(d * npair + q) * ld_out + p] = -0.5 (bra_i ket_{d,j} - bra_j ket_{d,i}), with
+ * bra_i = d_bra[i * ld_bra + p] and ket_{d,j} = d_ket[(d * nmo + j) * ld_ket + p]
+ * (orbkit's numpy rounding, bit for bit). */
+int okg_mo_pair_flux(int ndrv, int nmo, int npair, const int* d_pairs, const double* d_bra, int64_t ld_bra,
+                     const double* d_ket, int64_t ld_ket, int64_t npts, double* d_out, int64_t ld_out,
+                     okg_stream stream);
+
 /* ---------------------------------------------------------------- mixed path
  * rho and grad rho with the C.AO contraction on the tensor cores (tcgen05, BF16
  * operands split three ways, FP32 accumulation), exponent arguments and the final

@@ -54,6 +54,14 @@ SIGNATURES = {
     "okg_rho_mixed": (ctypes.c_int, [_vp, ctypes.POINTER(OkgGrid), ctypes.c_int, _vp, _vp, ctypes.c_int64, _vp]),
     "okg_mixed_status": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "okg_diag_fp64_fma_rate": (ctypes.c_int, [ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]),
+    "okg_mo_from_ao": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int64, ctypes.c_int64, _vp,
+                                      ctypes.c_int64, _vp]),
+    "okg_cart2sph": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_int64,
+                                    _vp, ctypes.c_int64, _vp]),
+    "okg_mo_products": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int64, _vp,
+                                       ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int64, _vp]),
+    "okg_mo_pair_flux": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_int64, _vp,
+                                        ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int64, _vp]),
 }
 
 

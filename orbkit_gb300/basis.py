@@ -137,7 +137,13 @@ class DeviceBasis:
         if C.shape[1] != self.nao:
             raise ValueError("MO coefficients have %d columns, the basis has %d AOs" % (C.shape[1], self.nao))
         if self.spherical:
-            C = C @ self.T_dev
+            # C_eff = C_sph . T by the FP64 contraction kernel (T's Cartesian columns
+            # play the role of grid points)
+            C = C.contiguous()
+            out = torch.empty((C.shape[0], self.ncart), dtype=torch.float64, device=self.device)
+            _lib.check(self._L.okg_mo_from_ao(C.shape[0], self.nao, _lib.ptr(C), _lib.ptr(self.T_dev), self.ncart,
+                                              self.ncart, _lib.ptr(out), self.ncart, _lib.stream_handle()))
+            return out
         return C.contiguous()
 
     def __del__(self):

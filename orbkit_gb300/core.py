@@ -208,37 +208,93 @@ def ao_creator(geo_spec, ao_spec, drv=None, x=None, y=None, z=None, is_vector=No
     return out.reshape((out.shape[0],) + N) if not vec else out
 
 
-def mo_creator(ao_list, mo_spec):
-    """MOs from given AO values, MO = C . AO (orbkit/core.py:107-132; cy_core.pyx:82-101).
+def _point_steps(npts, bytes_per_point):
+    """Point ranges of at most MAX_SLICE_BYTES of device buffers each."""
+    return [(i, j) for (i, j) in _slices(npts, bytes_per_point) if j > i]
 
-    The AO values are an input here, so this is a plain FP64 GEMM (cuBLAS through
-    torch) on the device; the fused paths never materialise AO values."""
+
+def mo_creator(ao_list, mo_spec):
+    """MOs from given AO values, MO = C . AO (orbkit/core.py:107-132; cy_core.pyx:82-101),
+    as the hand-written FP64 contraction okg_mo_from_ao on the device (points sliced
+    so that device buffers stay bounded).  The fused paths never materialise AOs."""
     torch = _torch()
+    L = _lib.load()
     ao_list = require(ao_list, "f")
     shape = ao_list.shape
     coeffs = require(mo_spec.get_coeffs(), "f")
+    if coeffs.ndim != 2 or coeffs.shape[1] != shape[0]:
+        raise ValueError("MO coefficients of shape %s do not match %d AOs" % (coeffs.shape, shape[0]))
+    A = ao_list.reshape(shape[0], -1)
+    npts = A.shape[1]
+    nmo, nao = coeffs.shape
     dev = torch.device("cuda", torch.cuda.current_device())
-    A = torch.from_numpy(ao_list.reshape(shape[0], -1)).to(dev)
     C = torch.from_numpy(coeffs).to(dev)
-    return (C @ A).cpu().numpy().reshape((len(coeffs),) + shape[1:])
+    out = numpy.empty((nmo, npts))
+    st = _lib.stream_handle()
+    for (i, j) in _point_steps(npts, 8 * (nao + nmo)):
+        a = torch.from_numpy(numpy.ascontiguousarray(A[:, i:j])).to(dev)
+        o = torch.empty((nmo, j - i), dtype=torch.float64, device=dev)
+        _lib.check(L.okg_mo_from_ao(nmo, nao, _lib.ptr(C), _lib.ptr(a), j - i, j - i, _lib.ptr(o), j - i, st))
+        out[:, i:j] = o.cpu().numpy()
+    return out.reshape((nmo,) + shape[1:])
 
 
 def cartesian2spherical(ao_list, ao_spec):
-    """Cartesian -> real spherical AOs (orbkit/core.py:135-176), as a device GEMM with
-    the transform T of orbkit's cart2sph table."""
+    """Cartesian -> real spherical AOs (orbkit/core.py:135-176): the kernel okg_cart2sph
+    applies orbkit's cart2sph combinations (Schlegel-Frisch table, last matching
+    Cartesian row, coefficient x global factor) term by term in orbkit's order, so
+    the result equals orbkit's bit for bit."""
     torch = _torch()
+    L = _lib.load()
     from .basis import spherical_csr
     ptr, idx, coef = spherical_csr(ao_spec)
-    ncart = len(ao_spec.get_lxlylz())
-    T = numpy.zeros((len(ptr) - 1, ncart))
-    for r in range(len(ptr) - 1):
-        for t in range(ptr[r], ptr[r + 1]):
-            T[r, idx[t]] += coef[t]
     ao_list = require(ao_list, "f")
     shape = ao_list.shape
+    ncart = shape[0]
+    if len(idx) and int(idx.max()) >= ncart:
+        raise ValueError("ao_list has %d rows, the basis lists %d Cartesian AOs" % (ncart, int(idx.max()) + 1))
+    nsph = len(ptr) - 1
+    A = ao_list.reshape(ncart, -1)
+    npts = A.shape[1]
     dev = torch.device("cuda", torch.cuda.current_device())
-    out = torch.from_numpy(T).to(dev) @ torch.from_numpy(ao_list.reshape(shape[0], -1)).to(dev)
-    return out.cpu().numpy().reshape((T.shape[0],) + shape[1:])
+    d_ptr, d_idx, d_coef = (torch.from_numpy(numpy.ascontiguousarray(v)).to(dev) for v in (ptr, idx, coef))
+    out = numpy.empty((nsph, npts))
+    st = _lib.stream_handle()
+    for (i, j) in _point_steps(npts, 8 * (ncart + nsph)):
+        a = torch.from_numpy(numpy.ascontiguousarray(A[:, i:j])).to(dev)
+        o = torch.empty((nsph, j - i), dtype=torch.float64, device=dev)
+        _lib.check(L.okg_cart2sph(nsph, ncart, _lib.ptr(d_ptr), _lib.ptr(d_idx), _lib.ptr(d_coef), _lib.ptr(a), j - i,
+                                  j - i, _lib.ptr(o), j - i, st))
+        out[:, i:j] = o.cpu().numpy()
+    return out.reshape((nsph,) + shape[1:])
+
+
+class _MoGrids:
+    """MO grids of one molecule on the device, one point range at a time (the
+    fused okg_eval_mo; AO values stay on chip)."""
+
+    def __init__(self, qc, x, y, z, vec, exact_mixed=False, mo_index=None):
+        torch = _torch()
+        self.L = _lib.load()
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        geo, ao_spec, mo_spec = unpack(qc)
+        self.b = get_basis(geo, ao_spec, self.dev)
+        coeffs = mo_spec.get_coeffs()
+        if mo_index is not None:
+            coeffs = coeffs[numpy.asarray(mo_index)]
+        self.C = self.b.c_eff(coeffs)
+        self.nmo = self.C.shape[0]
+        self.g = _DeviceGrid(x, y, z, vec, self.dev)
+        self.em = 1 if exact_mixed else 0
+
+    def __call__(self, codes, i, j):
+        """(len(codes), nmo, j - i) device tensor of the MOs' derivatives `codes`."""
+        torch = _torch()
+        gd, keep = self.g.slice(i, j)
+        o = torch.empty((len(codes), self.nmo, j - i), dtype=torch.float64, device=self.dev)
+        _lib.check(self.L.okg_eval_mo(self.b.handle, gd, self.nmo, _lib.ptr(self.C), len(codes),
+                                      _lib.int_array(codes), self.em, _lib.ptr(o), j - i, _lib.stream_handle()))
+        return o
 
 
 def _mixed_rho(qc, x, y, z, vec, N, drv):
@@ -357,8 +413,12 @@ def rho_compute_no_slice(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=F
     return ((ao_list, mo_list, rho, dao, dmo) + delta) if return_components else (rho,) + delta
 
 
-def calc_mo_matrix(qc_a, qc_b=None, drv=None, numproc=1, slice_length=1e4, save_hdf5=False, **kwargs):
-    """Products MO_a(r) * dMO_b(r) on the grid (orbkit/core.py:841-941)."""
+def calc_mo_matrix(qc_a, qc_b=None, drv=None, numproc=1, slice_length=1e4, save_hdf5=False, exact_mixed=False,
+                   **kwargs):
+    """Products MO_a(r) * dMO_b(r) on the grid module's grid (orbkit/core.py:841-941):
+    shape (NDRV, NMO_a, NMO_b) + grid shape.  The MO grids are evaluated and
+    multiplied on the device (okg_eval_mo, okg_mo_products); only the products come
+    back to the host."""
     if save_hdf5:
         raise NotImplementedError("save_hdf5 is not supported by the GPU path")
     ibra = [0]
@@ -371,17 +431,27 @@ def calc_mo_matrix(qc_a, qc_b=None, drv=None, numproc=1, slice_length=1e4, save_
     else:
         drv = [None] + drv
         iket = list(range(1, len(drv)))
-    if qc_b is None or qc_a is qc_b:
-        mo_ket = rho_compute(qc_a, calc_mo=True, drv=drv, **kwargs)
-        mo_bra = mo_ket[ibra]
-        mo_ket = mo_ket[iket]
-    else:
-        mo_bra = rho_compute(qc_a, calc_mo=True, drv=[drv[i] for i in ibra], **kwargs)
-        mo_ket = rho_compute(qc_b, calc_mo=True, drv=[drv[i] for i in iket], **kwargs)
-    nmo_a = mo_bra.shape[1]
-    nmo_b = mo_ket.shape[1]
-    out = numpy.zeros((mo_ket.shape[0], nmo_a) + mo_ket.shape[1:])
-    for n in range(nmo_a):
-        for m in range(nmo_b):
-            out[:, n, m] = mo_bra[:, n] * mo_ket[:, m]
-    return out
+    codes = [validate_drv(d) for d in drv]
+    if not grid.is_initialized:
+        grid.grid_init()
+    x, y, z, vec, N = _grid_arrays(grid.x, grid.y, grid.z, grid.is_vector, use_module=False)
+    same = qc_b is None or qc_a is qc_b
+    mo_a = _MoGrids(qc_a, x, y, z, vec, exact_mixed)
+    mo_b = mo_a if same else _MoGrids(qc_b, x, y, z, vec, exact_mixed)
+    na, nb, nk = mo_a.nmo, mo_b.nmo, len(iket)
+    npts = mo_a.g.npts
+    out = numpy.empty((nk, na, nb, npts))
+    L = _lib.load()
+    torch = _torch()
+    for (i, j) in _point_steps(npts, 8 * (nk * na * nb + (len(drv) + 1) * max(na, nb))):
+        if same:
+            m = mo_a(codes, i, j)
+            bra, ket = m[ibra[0]], m[iket].contiguous()
+        else:
+            bra = mo_a([codes[k] for k in ibra], i, j)[0]
+            ket = mo_b([codes[k] for k in iket], i, j)
+        o = torch.empty((nk, na, nb, j - i), dtype=torch.float64, device=mo_a.dev)
+        _lib.check(L.okg_mo_products(nk, na, nb, _lib.ptr(bra), j - i, _lib.ptr(ket), j - i, j - i, _lib.ptr(o),
+                                     j - i, _lib.stream_handle()))
+        out[..., i:j] = o.cpu().numpy()
+    return out.reshape((nk, na, nb) + N)

@@ -247,4 +247,15 @@ def test_mo_matrix_and_transition_flux(core):
         expect = -0.5 * (mo[0, i] * mo[1:, j] - mo[0, j] * mo[1:, i])
         assert_fp64_close(jmo[:, n], expect, "jmo %d %d" % (i, j))
     assert numpy.abs(jmo[:, 2]).max() == 0.0
+    # the product kernels round as numpy does: bit for bit on the GPU's own MO grids
+    mg = core.rho_compute(qc, calc_mo=True, drv=[None] + drv)
+    numpy.testing.assert_array_equal(mm, mg[0][None, :, None] * mg[1:][:, None, :])
+    for n, (i, j) in enumerate(pairs):
+        numpy.testing.assert_array_equal(jmo[:, n], -0.5 * (mg[0, i] * mg[1:, j] - mg[0, j] * mg[1:, i]))
+    # two molecules (bra from qc, ket from a second MO set on the same basis)
+    qc2 = synthetic.small(seed=5)["qc"]
+    mm2 = core.calc_mo_matrix(qc, qc2, drv="y")
+    mg2 = core.rho_compute(qc2, calc_mo=True, drv=["y"])
+    assert mm2.shape == (1, nmo, qc2.mo_spec.get_coeffs().shape[0], 7, 6, 5)
+    numpy.testing.assert_array_equal(mm2, mg[0][None, :, None] * mg2[:, None, :])
     grid.reset_grid()

@@ -74,6 +74,27 @@ def test_compute_entry_points_reject_null(lib):
                        None) == -1
 
 
+def test_grid_operation_entry_points_validate_arguments(lib):
+    """okg_mo_from_ao / okg_cart2sph / okg_mo_products / okg_mo_pair_flux reject NULL
+    pointers, empty counts and leading dimensions below npts before touching a device;
+    npts == 0 is a no-op."""
+    i64 = ctypes.c_int64
+    fake = ctypes.c_void_p(16)  # never dereferenced: rejected or zero-size before any device work
+    for f in ("okg_mo_from_ao", "okg_cart2sph", "okg_mo_products", "okg_mo_pair_flux"):
+        getattr(lib, f).restype = ctypes.c_int
+    assert lib.okg_mo_from_ao(0, 4, fake, fake, i64(8), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_from_ao(2, 4, None, fake, i64(8), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_from_ao(2, 4, fake, fake, i64(4), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_from_ao(2, 4, fake, fake, i64(8), i64(0), fake, i64(8), None) == 0
+    assert lib.okg_cart2sph(3, 0, fake, fake, fake, fake, i64(8), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_cart2sph(3, 5, fake, fake, fake, fake, i64(8), i64(9), fake, i64(8), None) == -1
+    assert lib.okg_mo_products(1, 2, 0, fake, i64(8), fake, i64(8), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_products(1, 2, 2, fake, i64(8), None, i64(8), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_pair_flux(3, 4, 1, None, fake, i64(8), fake, i64(8), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_pair_flux(3, 4, 1, fake, fake, i64(8), fake, i64(2), i64(8), fake, i64(8), None) == -1
+    assert lib.okg_mo_pair_flux(3, 4, 1, fake, fake, i64(8), fake, i64(8), i64(0), fake, i64(8), None) == 0
+
+
 def _overlap_plan(lib, lxlylz, ncart, nprim=None, atoms=None, natom=1):
     ip = lambda a: (ctypes.c_int * len(a))(*a)
     nshell = len(ncart)
