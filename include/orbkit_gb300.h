@@ -187,6 +187,12 @@ int okg_rho_mixed(okg_mixed_plan* plan, const okg_grid* grid, int want_grad, dou
 /* Synchronising check of the plan's device status word (bounded tensor-core waits):
  * OKG_ERR_TIMEOUT if a wait expired since the last check (the word is then cleared). */
 int okg_mixed_status(okg_mixed_plan* plan, int* device_status);
+/* Polls per bounded device wait of the plan's launches (default 2^24, >= 1).  When a
+ * wait expires the kernel raises the status word, stops issuing tensor-core work,
+ * waits for its own bulk copies and MMAs in flight, frees its tensor memory and
+ * returns (the outputs are then incomplete); the next launch starts afresh.  A small
+ * limit makes a wait expire on purpose, which is how the timeout path is tested. */
+int okg_mixed_plan_set_wait_limit(okg_mixed_plan* plan, long long polls);
 
 /* ------------------------------------------------------------------- batches
  * Many molecules with uneven point sets (e.g. atom-centred grids) in one

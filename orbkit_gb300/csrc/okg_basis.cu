@@ -154,6 +154,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     std::vector<int> comp_row;
     std::vector<double> comp_g;
     std::vector<int> prim_L;
+    std::vector<int> prim_atom;  // atom of each primitive (the AO kernel's per-axis tables)
     int ncart = 0, nprim = 0, max_np = 0, max_l = 0;
     int l_hist[OKG_MAX_L + 1] = {0};
     for (int s = 0; s < nshell; ++s) {
@@ -193,7 +194,10 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
             if (h_renorm) g *= h_renorm[ncart + r];
             comp_g[sh.comp0 + j] = g;
         }
-        for (int q = 0; q < np; ++q) prim_L.push_back(L);
+        for (int q = 0; q < np; ++q) {
+            prim_L.push_back(L);
+            prim_atom.push_back(at);
+        }
         ncart += nc;
         nprim += np;
         max_np = np > max_np ? np : max_np;
@@ -298,6 +302,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     const size_t o_prim = lay.take(sizeof(double) * 2 * nprim);
     const size_t o_prim32 = lay.take(sizeof(float) * 4 * nprim);
     const size_t o_primL = lay.take(sizeof(int) * nprim);
+    const size_t o_patom = lay.take(sizeof(int) * nprim);
     const size_t o_crow = lay.take(sizeof(int) * comp_row.size());
     const size_t o_cg = lay.take(sizeof(double) * comp_g.size());
     const size_t o_sptr = lay.take(sizeof(int) * sph_ptr.size());
@@ -319,6 +324,8 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     e = cudaMemset(blk, 0, bytes);
     if (e == cudaSuccess) e = cudaMemcpy(blk + o_shells, shells.data(), sizeof(Shell) * nshell, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(blk + o_primL, prim_L.data(), sizeof(int) * nprim, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(blk + o_patom, prim_atom.data(), sizeof(int) * nprim, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_crow, comp_row.data(), sizeof(int) * comp_row.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -349,6 +356,7 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     d.shells = (const Shell*)(blk + o_shells);
     d.prim = (const double*)(blk + o_prim);
     d.prim32 = (const float*)(blk + o_prim32);
+    d.prim_atom = (const int*)(blk + o_patom);
     d.comp_row = (const int*)(blk + o_crow);
     d.comp_g = (const double*)(blk + o_cg);
     d.sph_ptr = (const int*)(blk + o_sptr);

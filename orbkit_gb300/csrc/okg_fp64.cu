@@ -1,5 +1,5 @@
-// FP64 grid kernels: AO evaluation (okg_eval_ao) and the fused AO -> MO ->
-// density kernels (okg_eval_mo, okg_rho).
+// FP64 fused AO -> MO -> density kernels (okg_eval_mo, okg_rho); the AO
+// kernels of okg_eval_ao are in okg_ao.cu.
 //
 // Reference algorithm: orbkit/c_grid-based.c:9-79 (c_lcreator: per point, per
 // primitive exp, per Cartesian component the contraction times the polynomial or
@@ -15,61 +15,6 @@
 #include "okg_internal.cuh"
 
 namespace okg {
-
-struct DrvList {
-    int n;
-    int code[10];
-};
-
-// ------------------------------------------------------------------ AO kernel
-// One thread per point; shells are walked in order, the atom-relative position
-// and r^2 are recomputed only when the atom changes.
-template <bool SPH>
-__global__ void __launch_bounds__(128) ao_eval_kernel(BasisDev B, Grid g, DrvList drv, unsigned chmask, int mixed_ref,
-                                                      double* __restrict__ out, long long ld, int nao)
-{
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= g.npts) return;
-    double x, y, z;
-    grid_point(g, p, x, y, z);
-    const bool n1 = need_r1(chmask), n2 = need_r2(chmask);
-    int last_atom = -1;
-    double X = 0, Y = 0, Z = 0, rr = 0;
-    for (int s = 0; s < B.nshell; ++s) {
-        const Shell sh = B.shells[s];
-        if (sh.atom != last_atom) {
-            X = x - B.atoms[4 * sh.atom];
-            Y = y - B.atoms[4 * sh.atom + 1];
-            Z = z - B.atoms[4 * sh.atom + 2];
-            rr = X * X + Y * Y + Z * Z;
-            last_atom = sh.atom;
-        }
-        const Radial<double> r = radial64(B.prim, sh.prim0, sh.nprim, rr, n1, n2);
-        if (!SPH) {
-            shell_eval_L(sh.L, X, Y, Z, r, chmask, mixed_ref != 0, [&](int ch, int j, double v) {
-                const int row = B.comp_row[sh.comp0 + j];
-                if (row < 0) return;
-                const double gv = v * B.comp_g[sh.comp0 + j];
-                for (int d = 0; d < drv.n; ++d)
-                    if (drv.code[d] == ch) out[((long long)d * nao + sh.out0 + row) * ld + p] = gv;
-            });
-        } else {
-            for (int ch = 0; ch < 10; ++ch) {
-                if (!(chmask & (1u << ch))) continue;
-                double cv[OKG_MAX_NCART];
-                shell_eval_L(sh.L, X, Y, Z, r, 1u << ch, mixed_ref != 0,
-                             [&](int, int j, double v) { cv[j] = v * B.comp_g[sh.comp0 + j]; });
-                for (int o = 0; o < sh.nout; ++o) {
-                    const int row = sh.sph0 + o;
-                    double acc = 0.0;
-                    for (int t = B.sph_ptr[row]; t < B.sph_ptr[row + 1]; ++t) acc += B.sph_coef[t] * cv[B.sph_cidx[t]];
-                    for (int d = 0; d < drv.n; ++d)
-                        if (drv.code[d] == ch) out[((long long)d * nao + row) * ld + p] = acc;
-                }
-            }
-        }
-    }
-}
 
 // ------------------------------------------------------------- fused kernels
 // CTA = FP points x FG MO groups (64 x 4 = 256 threads; 8 x 16 for small point
@@ -294,63 +239,6 @@ static int dispatch_fused(const okg_basis* b, const Grid& g, const FusedArgs& A,
 }  // namespace okg
 
 using namespace okg;
-
-static int make_grid(const okg_grid* gr, Grid& g)
-{
-    if (!gr) return set_error(OKG_ERR_ARG, "grid is NULL");
-    g.x = gr->d_x;
-    g.y = gr->d_y;
-    g.z = gr->d_z;
-    g.npts = gr->npts;
-    g.offset = gr->offset;
-    g.nx = gr->nx;
-    g.ny = gr->ny;
-    g.nz = gr->nz;
-    g.regular = gr->regular;
-    if (g.npts < 0 || !g.x || !g.y || !g.z) return set_error(OKG_ERR_ARG, "grid: NULL coordinates or npts < 0");
-    if (g.regular) {
-        if (g.nx <= 0 || g.ny <= 0 || g.nz <= 0 || g.offset < 0 ||
-            g.offset + g.npts > (long long)g.nx * g.ny * g.nz)
-            return set_error(OKG_ERR_ARG, "grid: regular grid range outside Nx*Ny*Nz");
-    }
-    return OKG_OK;
-}
-
-static int make_drv(int ndrv, const int* h_drv, DrvList& d, unsigned& mask)
-{
-    if (ndrv < 0 || ndrv > 10 || (ndrv > 0 && !h_drv)) return set_error(OKG_ERR_ARG, "drv: 0..10 codes required");
-    d.n = ndrv;
-    mask = 0;
-    for (int i = 0; i < 10; ++i) d.code[i] = 0;
-    for (int i = 0; i < ndrv; ++i) {
-        if (h_drv[i] < 0 || h_drv[i] > 9) return set_error(OKG_ERR_DRV, "drv: code outside 0..9");
-        d.code[i] = h_drv[i];
-        mask |= 1u << h_drv[i];
-    }
-    return OKG_OK;
-}
-
-extern "C" int okg_eval_ao(const okg_basis* b, const okg_grid* grid, int ndrv, const int* h_drv, int exact_mixed,
-                           double* d_out, int64_t ld, okg_stream stream)
-{
-    if (!b || !d_out) return set_error(OKG_ERR_ARG, "okg_eval_ao: NULL basis or output");
-    Grid g;
-    int st = make_grid(grid, g);
-    if (st) return st;
-    DrvList d;
-    unsigned mask;
-    if ((st = make_drv(ndrv, h_drv, d, mask))) return st;
-    if (ndrv == 0 || g.npts == 0) return OKG_OK;
-    if (ld < g.npts) return set_error(OKG_ERR_ARG, "okg_eval_ao: ld < npts");
-    const unsigned nblk = (unsigned)((g.npts + 127) / 128);
-    if (b->dev.spherical)
-        ao_eval_kernel<true><<<nblk, 128, 0, (cudaStream_t)stream>>>(b->dev, g, d, mask, !exact_mixed, d_out, ld,
-                                                                    b->nao_out);
-    else
-        ao_eval_kernel<false><<<nblk, 128, 0, (cudaStream_t)stream>>>(b->dev, g, d, mask, !exact_mixed, d_out, ld,
-                                                                     b->nao_out);
-    return cuda_status(cudaGetLastError(), "okg_eval_ao launch");
-}
 
 extern "C" int okg_eval_mo(const okg_basis* b, const okg_grid* grid, int nmo, const double* d_coeff, int ndrv,
                            const int* h_drv, int exact_mixed, double* d_out, int64_t ld, okg_stream stream)

@@ -67,6 +67,7 @@ struct BasisDev {
     const Shell* shells;     // nshell
     const double* prim;      // nprim x 2 : alpha, w (w includes the alpha-dependent norm)
     const float* prim32;     // nprim x 4 : alpha*log2(e) (hi, lo), w (hi, lo) for the mixed path
+    const int* prim_atom;    // nprim : atom of each primitive
     const int* comp_row;     // per shell canonical component -> listed row within shell, or -1
     const double* comp_g;    // per shell canonical component -> angular norm factor x 'N'
     const int* sph_ptr;      // nsph + 1
@@ -257,4 +258,47 @@ struct okg_basis {
 namespace okg {
 int set_error(int status, const char* msg);
 int cuda_status(cudaError_t e, const char* where);
+
+// Requested derivative codes of a call (orbkit's drv codes 0..9).
+struct DrvList {
+    int n;
+    int code[10];
+};
+
+// okg_grid -> Grid with the checks every grid entry point makes.
+inline int make_grid(const okg_grid* gr, Grid& g)
+{
+    if (!gr) return set_error(OKG_ERR_ARG, "grid is NULL");
+    g.x = gr->d_x;
+    g.y = gr->d_y;
+    g.z = gr->d_z;
+    g.npts = gr->npts;
+    g.offset = gr->offset;
+    g.nx = gr->nx;
+    g.ny = gr->ny;
+    g.nz = gr->nz;
+    g.regular = gr->regular;
+    if (g.npts < 0 || !g.x || !g.y || !g.z) return set_error(OKG_ERR_ARG, "grid: NULL coordinates or npts < 0");
+    if (g.regular) {
+        if (g.nx <= 0 || g.ny <= 0 || g.nz <= 0 || g.offset < 0 ||
+            g.offset + g.npts > (long long)g.nx * g.ny * g.nz)
+            return set_error(OKG_ERR_ARG, "grid: regular grid range outside Nx*Ny*Nz");
+    }
+    return OKG_OK;
+}
+
+// Derivative codes -> DrvList and the mask of channels they need.
+inline int make_drv(int ndrv, const int* h_drv, DrvList& d, unsigned& mask)
+{
+    if (ndrv < 0 || ndrv > 10 || (ndrv > 0 && !h_drv)) return set_error(OKG_ERR_ARG, "drv: 0..10 codes required");
+    d.n = ndrv;
+    mask = 0;
+    for (int i = 0; i < 10; ++i) d.code[i] = 0;
+    for (int i = 0; i < ndrv; ++i) {
+        if (h_drv[i] < 0 || h_drv[i] > 9) return set_error(OKG_ERR_DRV, "drv: code outside 0..9");
+        d.code[i] = h_drv[i];
+        mask |= 1u << h_drv[i];
+    }
+    return OKG_OK;
+}
 }  // namespace okg

@@ -138,12 +138,22 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
 }
 
 // Bounded wait: returns false (and raises the status word) if the phase does not
-// complete within WAIT_LIMIT polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status)
+// complete within `limit` polls (WAIT_LIMIT unless the plan sets another).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status, long long limit)
+{
+    for (long long it = 0; it < limit; ++it)
+        if (mbar_try(bar, parity)) return true;
+    atomicExch(status, 1);
+    return false;
+}
+
+// Wait for the completion of the CTA's own asynchronous work (a bulk copy or
+// MMAs) before it leaves: bounded by WAIT_LIMIT whatever the plan's limit, since
+// such work always completes; false if even that expires.
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity)
 {
     for (long long it = 0; it < WAIT_LIMIT; ++it)
         if (mbar_try(bar, parity)) return true;
-    atomicExch(status, 1);
     return false;
 }
 
@@ -288,6 +298,7 @@ struct Params {
     MolDesc D;
     int* status;                  // device status word: 1 = timeout
     unsigned long long* counter;  // tile counter, zero at launch (tiles are handed out dynamically)
+    long long wait_limit;         // polls per bounded wait
 };
 
 // Screening: a primitive is skipped for a tile when alpha log2(e) d^2 > SCREEN_LOG2,
@@ -308,6 +319,8 @@ struct CtaState {
     uint32_t bar_acc_empty;      // every generation thread has read the accumulators
     uint32_t bar_screened;       // NBUF mbarriers (tile buffers): tile index and screening tables written
     uint32_t bar_kfree;          // NBUF mbarriers: generation threads and MMA warp are done with the buffer's tile
+    uint32_t bar_drain;          // the MMA warp's last commit: every MMA it issued is complete
+    long long wait_limit;        // polls per bounded wait
     uint32_t tmem;
     int* abort_flag;
     unsigned char* nkeep;        // NBUF x MAX_SHELLS: per shell, kept primitives | owning generation group << 5
@@ -456,7 +469,7 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
     long long gnext = 0, gend = 0, gpend = -1;
     for (uint32_t ord = 0;; ++ord) {
         const int b = tbuf(ord);
-        if (ord >= NBUF && !mbar_wait(S.bar_kfree + 8 * b, tphase(ord - NBUF), status)) *S.abort_flag = 1;
+        if (ord >= NBUF && !mbar_wait(S.bar_kfree + 8 * b, tphase(ord - NBUF), status, S.wait_limit)) *S.abort_flag = 1;
         long long t = -1;
         int mol = 0;
         // the counter increment for the following tile (or range) is issued one
@@ -604,7 +617,8 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int b = tbuf(ord);
-    if (!mbar_wait(S.bar_screened + 8 * b, tphase(ord), status)) {
+    if (*S.abort_flag) return -1;
+    if (!mbar_wait(S.bar_screened + 8 * b, tphase(ord), status, S.wait_limit)) {
         *S.abort_flag = 1;
         return -1;
     }
@@ -690,7 +704,7 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
     const int grp = tid / (128 / P);
     const uint32_t s = seq & 1u, u = seq >> 1;
     unsigned char* A_s = S.A_s + s * A_STAGE;
-    if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
+    if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status, S.wait_limit)) *S.abort_flag = 1;
     const int4 ck = B.mchunks[c];
     Shell nx = load_shell(B.shells + ck.x);  // records are loaded one shell ahead
     for (int si = ck.x; si < ck.y; ++si) {
@@ -781,10 +795,10 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
     bool own[4];
 #pragma unroll
     for (int o = 0; o < 4; ++o) own[o] = (o % E == h) && (o == 0 || D.want_grad);
-    if (!mbar_wait(S.bar_acc_full, accseq & 1u, status)) *S.abort_flag = 1;
+    if (!mbar_wait(S.bar_acc_full, accseq & 1u, status, S.wait_limit)) *S.abort_flag = 1;
     ++accseq;
     tc_fence_after();
-    if (own[0] || own[1] || own[2] || own[3]) {
+    if ((own[0] || own[1] || own[2] || own[3]) && !*S.abort_flag) {
         const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
         const float2* occf = D.occf + pass * npad;
         const float2* occ2f = D.occf + (D.npass + pass) * npad;
@@ -867,7 +881,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
             const BasisDev& B = Dg.B;
             const unsigned char* nkeep = S.nkeep + tbuf(ord) * MAX_SHELLS;
-            while (c >= 0) {
+            while (c >= 0 && !*S.abort_flag) {
                 gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
                 ++nch;
                 nks += ksteps_of(km[c]);
@@ -973,7 +987,7 @@ __device__ __forceinline__ bool mma_open_next(const CtaState& S, MmaItem& it, bo
         }
         release = true;
         const int b = tbuf(it.ord);
-        if (!mbar_wait(S.bar_screened + 8 * b, tphase(it.ord), status)) *S.abort_flag = 1;
+        if (!mbar_wait(S.bar_screened + 8 * b, tphase(it.ord), status, S.wait_limit)) *S.abort_flag = 1;
         if (S.tile_slot[b] < 0 || *S.abort_flag) return false;
         const MolDesc& D = S.mol[BATCH ? b : 0];
         it.bpack = D.bpack;
@@ -988,14 +1002,18 @@ __device__ __forceinline__ bool mma_open_next(const CtaState& S, MmaItem& it, bo
 }
 
 // MMA warp, lane 0: the bulk copy of an item's B block into stage seq % 2 once
-// that stage's previous MMAs are complete.
-__device__ __forceinline__ void mma_prefetch_b(const CtaState& S, const MmaItem& it, uint32_t seq, int* status)
+// that stage's previous MMAs are complete.  Nothing is issued once the CTA has
+// aborted (or if the stage does not free up): returns whether the copy is in
+// flight, so that the warp can wait for it before the CTA leaves.
+__device__ __forceinline__ bool mma_prefetch_b(const CtaState& S, const MmaItem& it, uint32_t seq, int* status)
 {
     const uint32_t s = seq & 1u, u = seq >> 1;
     const int bunits = 3 * it.npad * RUNITS;
-    if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status)) *S.abort_flag = 1;
+    if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status, S.wait_limit)) *S.abort_flag = 1;
+    if (*S.abort_flag) return false;
     bulk_load(smem_u32(S.B_s + s * B_STAGE), it.bpack + ((long long)it.pass * it.nmchunk + it.c) * bunits,
               (uint32_t)bunits * 16u, S.bar_bload + 8 * s);
+    return true;
 }
 
 // MMA side of the CTA (the last warp): for every kept chunk in order, the column
@@ -1009,15 +1027,25 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
     uint32_t seq = 0, accseq = 0;
     MmaItem cur;
     cur.ord = 0;
+    // lane 0: sequence number of a bulk copy in flight that no wait has seen land
+    // (-1: none), and whether any MMA was issued -- both drained before the CTA leaves
+    long long pend = -1;
+    bool issued = false;
     bool have = mma_open_next<BATCH>(S, cur, false, status);
-    if (have && lane == 0) mma_prefetch_b(S, cur, seq, status);
+    if (have && lane == 0 && mma_prefetch_b(S, cur, seq, status)) pend = seq;
     int kq = 0;  // K-steps issued in the current job
-    while (have) {
+    // (loop exits are decided by lane 0 and broadcast: the warp leaves together)
+    while (__shfl_sync(0xffffffffu, (int)(have && !*S.abort_flag), 0)) {
         const uint32_t s = seq & 1u, u = seq >> 1;
         unsigned char* B_s = S.B_s + s * B_STAGE;
         const int npad = cur.npad;
         const int bunits = 3 * npad * RUNITS;
-        if (!mbar_wait(S.bar_bload + 8 * s, u & 1u, status)) *S.abort_flag = 1;
+        const bool landed = mbar_wait(S.bar_bload + 8 * s, u & 1u, status, S.wait_limit);
+        if (!__all_sync(0xffffffffu, landed)) {
+            *S.abort_flag = 1;
+            break;
+        }
+        if (pend == (long long)seq) pend = -1;
         // columns of screened shells are zeroed.  Lane l touches the 16-byte units
         // l, l + 32, ...: rows n = l / 4 (mod 8) of every part, physical unit l % 4, so
         // with rows of 4 units and the 64-byte swizzle (unit ^ (n >> 1) % 4) always the
@@ -1045,8 +1073,9 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
         __syncwarp();
         if (lane == 0) {
             // the previous job's accumulators must have been read before they are overwritten
-            if (kq == 0 && accseq > 0 && !mbar_wait(S.bar_acc_empty, (accseq - 1) & 1u, status)) *S.abort_flag = 1;
-            if (!mbar_wait(S.bar_full + 8 * s, u & 1u, status)) *S.abort_flag = 1;
+            if (kq == 0 && accseq > 0 && !mbar_wait(S.bar_acc_empty, (accseq - 1) & 1u, status, S.wait_limit))
+                *S.abort_flag = 1;
+            if (!mbar_wait(S.bar_full + 8 * s, u & 1u, status, S.wait_limit)) *S.abort_flag = 1;
             tc_fence_after();
             const int nch = cur.nch;
             const int pf = nch > 2 ? 1 : nch - 1;  // channel after which the next B block is requested
@@ -1083,12 +1112,12 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
                             mma_bf16(S.tmem + col * npad, ad, bd, idesc, accf);
                         }
                     }
-                    if (ch == pf && in_tile) mma_prefetch_b(S, nxt, seq + 1, status);
+                    if (ch == pf && in_tile && mma_prefetch_b(S, nxt, seq + 1, status)) pend = seq + 1;
                 }
+                issued = true;
                 mma_commit(S.bar_empty + 8 * s);
             } else {
                 mbar_arrive(S.bar_empty + 8 * s);
-                if (in_tile) mma_prefetch_b(S, nxt, seq + 1, status);
             }
             if (!in_tile || nxt.pass != cur.pass) {
                 // last chunk of the job: hand the accumulators to the epilogue
@@ -1110,26 +1139,38 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
             // leave the tile once its last chunk's MMAs are issued; the next tile's
             // first B block is requested as soon as the tile is open
             have = mma_open_next<BATCH>(S, nxt, true, status);
-            if (have && lane == 0) mma_prefetch_b(S, nxt, seq, status);
+            if (have && lane == 0 && mma_prefetch_b(S, nxt, seq, status)) pend = seq;
         }
         cur = nxt;
     }
+    // before the CTA leaves (normally or after an expired wait): the bulk copy still
+    // in flight lands and every issued MMA completes, so that no asynchronous write
+    // reaches shared or tensor memory after the teardown
+    __syncwarp();
+    if (lane == 0) {
+        if (pend >= 0) mbar_drain(S.bar_bload + 8 * (uint32_t)(pend & 1), (uint32_t)(pend >> 1) & 1u);
+        if (issued) {
+            mma_commit(S.bar_drain);
+            mbar_drain(S.bar_drain, 0);
+        }
+    }
+    __syncwarp();
 }
 
 // CTA set-up shared by the kernels: shared-memory carve-up, A stages zeroed
 // (columns of screened shells keep stale but finite values, multiplied by zeroed B
 // columns), mbarriers, TMEM allocation.  NTT threads in all, NTG of them generate.
 template <int NTT, int NTG>
-__device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol, uint32_t tm_cols)
+__device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol, uint32_t tm_cols, long long wait_limit)
 {
     const int tid = threadIdx.x, warp = tid >> 5;
     CtaState S;
     S.A_s = smem;
     S.B_s = smem + NSTAGE * A_STAGE;
     S.kmask = (unsigned*)(S.B_s + NSTAGE * B_STAGE);
-    // full[2], empty[2], bload[2], acc full, acc empty, screened[NBUF], kfree[NBUF]
+    // full[2], empty[2], bload[2], acc full, acc empty, screened[NBUF], kfree[NBUF], drain
     uint64_t* bar = (uint64_t*)(S.kmask + NBUF * MAX_CHUNKS);
-    S.tile_slot = (long long*)(bar + 8 + 2 * NBUF);
+    S.tile_slot = (long long*)(bar + 9 + 2 * NBUF);
     uint32_t* tmem_slot = (uint32_t*)(S.tile_slot + NBUF);
     S.abort_flag = (int*)(tmem_slot + 1);
     S.nkeep = (unsigned char*)(S.abort_flag + 1);
@@ -1141,6 +1182,8 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
     S.bar_acc_empty = smem_u32(bar + 7);
     S.bar_screened = smem_u32(bar + 8);
     S.bar_kfree = smem_u32(bar + 8 + NBUF);
+    S.bar_drain = smem_u32(bar + 8 + 2 * NBUF);
+    S.wait_limit = wait_limit;
     for (int i = tid; i < NSTAGE * A_STAGE / 16; i += NTT) ((uint4*)S.A_s)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
@@ -1154,6 +1197,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
             mbar_init(S.bar_screened + 8 * b, 32);     // the tile warp
             mbar_init(S.bar_kfree + 8 * b, NTG + 1);   // every generation thread and the MMA warp
         }
+        mbar_init(S.bar_drain, 1);
         *S.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -1171,7 +1215,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
 }
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
-constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * NBUF * MAX_CHUNKS + (8 + 2 * NBUF) * 8 +
+constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * NBUF * MAX_CHUNKS + (9 + 2 * NBUF) * 8 +
                               NBUF * 8 + 4 + 4 + NBUF * MAX_SHELLS + 64;
 static_assert(SMEM_BYTES + NBUF * sizeof(MolDesc) <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 static_assert(KC == 32, "column masks are 32-bit and operand rows one 64-byte swizzle row");
@@ -1241,7 +1285,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_kernel(const __
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
     if (threadIdx.x < sizeof(MolDesc) / 16) ((uint4*)mol)[threadIdx.x] = ((const uint4*)&P.D)[threadIdx.x];
     const uint32_t tm_cols = tmem_cols_for(P.D.npad);
-    CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, tm_cols);
+    CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, tm_cols, P.wait_limit);
     TileFeed F;
     F.counter = P.counter;
     F.ntiles = P.D.ntiles;
@@ -1268,6 +1312,7 @@ struct BatchParams {
     long long total_tiles;
     unsigned long long* counter;
     int* status;
+    long long wait_limit;
 };
 
 template <int NTG, int PP>
@@ -1275,7 +1320,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(co
 {
     __shared__ MolDesc mol[NBUF];
     unsigned char* smem = (unsigned char*)(((uintptr_t)mx_smem_raw + 1023) & ~(uintptr_t)1023);
-    CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, 512);
+    CtaState S = cta_setup<cta_threads(NTG), NTG>(smem, mol, 512, P.wait_limit);
     TileFeed F;
     F.counter = P.counter;
     F.ntiles = P.total_tiles;
@@ -1416,6 +1461,7 @@ struct okg_mixed_plan {
     int sm_count;
     size_t smem;
     int layout;  // index into GEN_LAYOUTS (generation threads, points per thread)
+    long long wait_limit;  // polls per bounded device wait (WAIT_LIMIT by default)
 };
 
 extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_max, okg_mixed_plan** out);
@@ -1463,6 +1509,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->sm_count = sms;
     p->smem = mx::SMEM_BYTES;
     p->layout = mx::LAYOUT_DEFAULT;
+    p->wait_limit = mx::WAIT_LIMIT;
     e = mx::configure_kernels();
     if (e != cudaSuccess) {
         cudaFree(p->block);
@@ -1488,6 +1535,13 @@ extern "C" int okg_mixed_plan_set_generation(okg_mixed_plan* p, int threads, int
         return set_error(OKG_ERR_ARG, "okg_mixed_plan_set_generation: (threads, points) must be (256|384|512, 1) or "
                                       "(256|384, 2)");
     p->layout = l;
+    return OKG_OK;
+}
+
+extern "C" int okg_mixed_plan_set_wait_limit(okg_mixed_plan* p, long long polls)
+{
+    if (!p || polls < 1) return set_error(OKG_ERR_ARG, "okg_mixed_plan_set_wait_limit: NULL plan or polls < 1");
+    p->wait_limit = polls;
     return OKG_OK;
 }
 
@@ -1535,6 +1589,7 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     mx::make_desc(P.D, p->basis->dev, g, p->bpack, p->occ, p->npass, p->npad, p->nmo, want_grad, d_rho, d_grad, ld);
     P.status = p->status;
     P.counter = (unsigned long long*)((char*)p->status + 64);
+    P.wait_limit = p->wait_limit;
     {
         cudaError_t e0 = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), (cudaStream_t)stream);
         if (e0 != cudaSuccess) return cuda_status(e0, "okg_rho_mixed: counter reset");
@@ -1676,6 +1731,7 @@ extern "C" int okg_batch_run(okg_batch* b, okg_stream stream)
     P.total_tiles = b->total_tiles;
     P.counter = b->d_counter;
     P.status = b->d_status;
+    P.wait_limit = mx::WAIT_LIMIT;
     const long long grid = b->total_tiles < b->ctas ? b->total_tiles : b->ctas;
     mx::launch_batch(b->layout, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_batch_run launch");
@@ -1838,6 +1894,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     make_desc(P.D, B, g, bpack, occ, npass, npad, nmo, want_grad, d_rho, d_grad, ld);
     P.status = status;
     P.counter = (unsigned long long*)(nd->base + st_off + 64);
+    P.wait_limit = WAIT_LIMIT;
     e = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: counter reset");
     const long long grid = P.D.ntiles < nd->sm_count ? P.D.ntiles : nd->sm_count;

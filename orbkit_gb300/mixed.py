@@ -31,6 +31,7 @@ _SIGS = {
     "okg_mixed_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "okg_mixed_plan_set_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "okg_mixed_plan_set_generation": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "okg_mixed_plan_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
 }
 
 
@@ -72,6 +73,10 @@ class MixedPlan:
         """Generation threads per CTA and grid points per generation thread:
         (256|384|512, 1) or (256|384, 2)."""
         _lib.check(self._L.okg_mixed_plan_set_generation(self._h, int(threads), int(points_per_thread)))
+
+    def set_wait_limit(self, polls):
+        """Polls per bounded device wait (default 2^24); an expired wait makes check() raise."""
+        _lib.check(self._L.okg_mixed_plan_set_wait_limit(self._h, int(polls)))
 
     @property
     def handle(self):
