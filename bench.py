@@ -8,10 +8,12 @@ Workload (default): the mid-size molecule -- 20 atoms (C/N/O/H 6:1:1:12) in a
   value      points/s of the mixed-precision path (tensor-core contraction, FP64
              exponent arguments and density accumulation, FP64 cusp region), inputs
              resident in HBM, L2 flushed (256 MB write) between timed steps.
-  e2e        the same through the public evaluator with host buffers: every step
-             uploads geometry, primitives, MO coefficients, occupations and grid
-             vectors from pinned host memory and reads rho + grad back into pinned
-             host memory.
+  e2e        the same through orbkit's drop-in call core.rho_compute(qc,
+             drv=['x','y','z'], precision='mixed') on the grid module's axes: grid
+             axes uploaded, rho + grad rho returned as numpy arrays every step (the
+             evaluator is reused from the first call on the molecule and grid); the
+             evaluator path that uploads every parameter each step from pinned host
+             memory is reported beside it.
   roofline   of the dominant kernel (the fused mixed kernel), achieved = algorithmic
              contraction FLOPs (8 NMO NAO per point) / its CUDA-event launch time.
   cpu_baseline  the CPU oracle (a C restatement of orbkit's cy_core/c_grid-based
@@ -122,12 +124,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_rate(qc, gx, gy, gz, target_s=12.0, seed=0, max_pts=2_000_000):
-    """Oracle points/s on a random sample of the regular grid (all host threads)."""
+def cpu_rate(qc, gx, gy, gz, target_s=12.0, seed=0, max_pts=2_000_000, nthreads=None):
+    """Oracle points/s on a random sample of the regular grid (all host threads, or
+    nthreads)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import okref
     okref.build()
-    cores = len(os.sched_getaffinity(0))
+    cores = nthreads or len(os.sched_getaffinity(0))
     rng = numpy.random.default_rng(seed)
 
     def sample(n):
@@ -270,7 +273,30 @@ def run_ours(args):
         plan.rho(gd, rho, grad, npts)
     kms, _, _ = timed(kernel_only, max(3, args.steps), 1)
 
-    # end to end through the evaluator with pinned host buffers
+    # end to end through orbkit's drop-in call, as an orbkit user makes it: the grid
+    # module holds the 160^3 axes (numpy), core.rho_compute(qc, drv=['x','y','z'],
+    # precision='mixed') uploads them, evaluates (tensor-core kernel + FP64 cusp
+    # points; the evaluator, its plan and the cusp points are reused from the first
+    # call on this molecule and grid) and returns numpy rho and grad rho
+    from orbkit_gb300 import core as okcore, grid as okgrid
+    okgrid.set_grid(gx, gy, gz, is_vector=False)
+    okcore.quiet = True
+
+    def step_dropin():
+        okcore.rho_compute(qc, drv=["x", "y", "z"], precision="mixed")
+
+    for _ in range(args.warmup):
+        step_dropin()
+    sync_all()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        step_dropin()
+    sync_all()
+    dropin_ms = (time.perf_counter() - te) * 1e3 / args.steps
+    dropin_h2d = 8 * (len(gx) + len(gy) + len(gz))
+
+    # end to end through the evaluator with pinned host buffers, every parameter
+    # (geometry, primitives, MO coefficients, occupations) uploaded every step
     prim_h = torch.from_numpy(b.flat["prim"].copy()).pin_memory()
     geo_h = torch.from_numpy(numpy.asarray(qc.geo_spec, dtype=numpy.float64).copy()).pin_memory()
     C_h = torch.from_numpy(qc.mo_spec.get_coeffs()).pin_memory()
@@ -293,10 +319,10 @@ def run_ours(args):
     h2d = (geo_h.numel() + prim_h.numel() + C_h.numel() + occ_h.numel() + sum(len(v) for v in gvec)) * 8
     d2h = 4 * npts * 8
 
-    times = torch.tensor([ms, kms, e2e_ms, fp64_ms], dtype=torch.float64, device=dev)
+    times = torch.tensor([ms, kms, e2e_ms, fp64_ms, dropin_ms], dtype=torch.float64, device=dev)
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    ms, kms, e2e_ms, fp64_ms = [float(v) for v in times.cpu()]
+    ms, kms, e2e_ms, fp64_ms, dropin_ms = [float(v) for v in times.cpu()]
     if rank != 0:
         return
 
@@ -348,14 +374,24 @@ def run_ours(args):
             "fp64_fma_peak_per_s": fp64_fma_peak(), "fp64_fma_diag_per_s": fma,
         },
         "clocks": clk,
-        "e2e": {"value": world * npts / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": world * npts / (dropin_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(dropin_h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": dropin_ms,
+                "api": "orbkit_gb300.core.rho_compute(qc, drv=['x','y','z'], precision='mixed') on the grid "
+                       "module's 160^3 axes, numpy results",
+                "evaluator_all_parameters_uploaded": {
+                    "value": world * npts / (e2e_ms * 1e-3), "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "api": "mixed.MixedEvaluator.update + evaluate, pinned host buffers"}},
         "gpu_launches": args.steps * (1 + (1 if n_fix else 0)),
     }
     if world == 1 and not args.no_cpu_baseline:
         rate, cores, n, dt = cpu_rate(qc, gx, gy, gz)
+        rate1, _, n1, dt1 = cpu_rate(qc, gx, gy, gz, target_s=4.0, seed=1, nthreads=1)
         out["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": "%d random points of the 160^3 grid, rho + grad rho, %.1f s" % (n, dt)}
+                               "sample": "%d random points of the 160^3 grid, rho + grad rho, %.1f s" % (n, dt),
+                               "single_core": {"value": rate1, "cores": 1,
+                                               "sample": "%d random points, one thread (numproc=1), %.1f s"
+                                                         % (n1, dt1)}}
     print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -225,7 +225,8 @@ int okg_batch_status(okg_batch* batch, int* device_status);
  * orbkit/c_support.c:28-188); AO tiles are recomputed, not stored.
  * Outputs (overwritten): d_dcoeff (nmo x ncart, w.r.t. C_eff), d_dprim (nprim x 2:
  * d/dalpha, d/dc in ao_spec.get_prim_coeffs() order), d_dgeo (natom x 3).
- * precision: 64 or 32 (arithmetic of the backward).  nmo <= 48.  d_work is caller
+ * precision: 64 or 32 (arithmetic of the backward).  Any nmo: above 48 MOs the AO
+ * tiles of the MO pass are recomputed per block of 48 MOs.  d_work is caller
  * memory of at least okg_rho_backward_workspace bytes (per-CTA partial sums,
  * reduced in a fixed order: results are deterministic). */
 int okg_rho_backward_workspace(const okg_basis* basis, const okg_grid* grid, int nmo, int precision, size_t* bytes);

@@ -19,7 +19,8 @@
 //
 // Tile: 32 points x 8 warps.  Phase 1 (per chunk of shells): AO value + gradient
 // in shared memory, MO value + gradient accumulated per warp (6 MOs each) -> W, V
-// in shared memory.  Phase 2 (per chunk again): AO value, gradient and all second
+// in shared memory; with more than 48 MOs, phase 1 runs once per block of 48 MOs
+// and W, V go to the CTA's slot of the workspace.  Phase 2 (per chunk again): AO value, gradient and all second
 // derivatives; A, B, G per (column, point); the dC pairs; per shell the exponent,
 // coefficient and nuclear terms, reduced over the warp's 32 points.  Partial sums
 // go to per-CTA slots of the caller's workspace (no atomics) and a second kernel
@@ -51,6 +52,7 @@ struct Args {
     T* part_c;  // [nblk][nmo][ncart]
     T* part_p;  // [nblk][nprim][2]
     T* part_g;  // [nblk][NW][natom][3]
+    T* part_w;  // nmo > NMOMAX: [nblk][2][nmo][P] (W and V of the CTA's tile), else null
     long long ntiles;
 };
 
@@ -134,7 +136,7 @@ __device__ __forceinline__ void shell_sums_L(int L, T X, T Y, T Z, T gx, T gy, T
     }
 }
 
-template <typename T>
+template <typename T, bool BIG>
 __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev B, Grid g, Args<T> A)
 {
     extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -147,6 +149,19 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
     T* G_s = B_s + KC * P;           // KC x P
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long blk = blockIdx.x;
+    // up to NMOMAX MOs: W, V and the coefficient chunks in shared memory; more MOs:
+    // W, V in the CTA's slot of the workspace and the coefficients read from global
+    // memory, the MOs of phase 1 formed in blocks of NMOMAX (AO tiles recomputed
+    // per block)
+    T* Wv;
+    T* Vv;
+    if constexpr (BIG) {
+        Wv = A.part_w + blk * 2ll * A.nmo * P;
+        Vv = Wv + (long long)A.nmo * P;
+    } else {
+        Wv = W_s;
+        Vv = V_s;
+    }
     T* pc = A.part_c + blk * (long long)A.nmo * B.ncart;
     T* pp = A.part_p + blk * 2ll * B.nprim;
     T* pg = A.part_g + blk * (long long)NW * B.natom * 3;
@@ -166,7 +181,8 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
         const T gy = (valid && A.g_grad) ? (T)A.g_grad[A.ld + p] : T(0);
         const T gz = (valid && A.g_grad) ? (T)A.g_grad[2 * A.ld + p] : T(0);
 
-        // ---------------- phase 1: MOs and their gradients
+        // ---------------- phase 1: MOs and their gradients (blocks of NMOMAX MOs)
+        for (int mb0 = 0; mb0 < A.nmo; mb0 += NMOMAX) {
         T acc[MB][4];
 #pragma unroll
         for (int m = 0; m < MB; ++m)
@@ -178,7 +194,7 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
             __syncthreads();
             for (int i = tid; i < NMOMAX * KC; i += NT) {
                 const int m = i / KC, kk = i % KC;
-                C_s[i] = (m < A.nmo && kk < kc) ? (T)A.C[(long long)m * B.ncart + ck.z + kk] : T(0);
+                C_s[i] = (mb0 + m < A.nmo && kk < kc) ? (T)A.C[(long long)(mb0 + m) * B.ncart + ck.z + kk] : T(0);
             }
             for (int s = ck.x + warp; s < ck.y; s += NW) {
                 const Shell sh = B.shells[s];
@@ -211,15 +227,18 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
         }
 #pragma unroll
         for (int m = 0; m < MB; ++m) {
-            const int mo = warp * MB + m;
+            const int mo = mb0 + warp * MB + m;
             T w = T(0), v = T(0);
             if (mo < A.nmo) {
                 const T o2 = T(2) * (T)A.occ[mo];
                 w = o2 * (gr * acc[m][0] + gx * acc[m][1] + gy * acc[m][2] + gz * acc[m][3]);
                 v = o2 * acc[m][0];
             }
-            W_s[mo * P + lane] = w;
-            V_s[mo * P + lane] = v;
+            if (mo < A.nmo || !BIG) {
+                Wv[mo * P + lane] = w;
+                Vv[mo * P + lane] = v;
+            }
+        }
         }
 
         // ---------------- phase 2: gradients
@@ -227,10 +246,11 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
             const int4 ck = B.chunks[ci];
             const int kc = ck.w - ck.z;
             __syncthreads();
-            for (int i = tid; i < NMOMAX * KC; i += NT) {
-                const int m = i / KC, kk = i % KC;
-                C_s[i] = (m < A.nmo && kk < kc) ? (T)A.C[(long long)m * B.ncart + ck.z + kk] : T(0);
-            }
+            if constexpr (!BIG)
+                for (int i = tid; i < NMOMAX * KC; i += NT) {
+                    const int m = i / KC, kk = i % KC;
+                    C_s[i] = (m < A.nmo && kk < kc) ? (T)A.C[(long long)m * B.ncart + ck.z + kk] : T(0);
+                }
             for (int s = ck.x + warp; s < ck.y; s += NW) {
                 const Shell sh = B.shells[s];
                 const T X = (T)(xd - B.atoms[4 * sh.atom]);
@@ -251,9 +271,13 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
             for (int kk = warp; kk < kc; kk += NW) {
                 T a = T(0), b = T(0);
                 for (int i = 0; i < A.nmo; ++i) {
-                    const T c = C_s[i * KC + kk];
-                    a += c * W_s[i * P + lane];
-                    b += c * V_s[i * P + lane];
+                    T c;
+                    if constexpr (BIG)
+                        c = (T)__ldg(A.C + (long long)i * B.ncart + ck.z + kk);
+                    else
+                        c = C_s[i * KC + kk];
+                    a += c * Wv[i * P + lane];
+                    b += c * Vv[i * P + lane];
                 }
                 A_s[kk * P + lane] = a;
                 B_s[kk * P + lane] = b;
@@ -268,7 +292,7 @@ __global__ void __launch_bounds__(NT, ctas_per_sm<T>()) adjoint_kernel(BasisDev 
                 T sacc = T(0);
                 for (int t = 0; t < P; ++t) {
                     const int pt = (t + lane) & (P - 1);
-                    sacc += W_s[i * P + pt] * AO_s[kk * P + pt] + V_s[i * P + pt] * G_s[kk * P + pt];
+                    sacc += Wv[i * P + pt] * AO_s[kk * P + pt] + Vv[i * P + pt] * G_s[kk * P + pt];
                 }
                 pc[(long long)i * B.ncart + ck.z + kk] += sacc;
             }
@@ -340,7 +364,9 @@ __global__ void reduce_kernel(const T* __restrict__ part, long long n, int nblk,
 template <typename T>
 size_t workspace_bytes(const okg_basis* b, int nmo, int nblk)
 {
-    return (size_t)nblk * ((size_t)nmo * b->ncart + 2 * (size_t)b->nprim + (size_t)NW * b->natom * 3) * sizeof(T) + 256;
+    const size_t wv = nmo > NMOMAX ? 2 * (size_t)nmo * P : 0;  // W and V of the CTA's tile
+    return (size_t)nblk * ((size_t)nmo * b->ncart + 2 * (size_t)b->nprim + (size_t)NW * b->natom * 3 + wv) * sizeof(T) +
+           256;
 }
 
 template <typename T>
@@ -373,15 +399,22 @@ static int run(const okg_basis* b, const Grid& g, int nmo, const double* C, cons
     A.part_c = (T*)work;
     A.part_p = A.part_c + (size_t)nblk * nmo * b->ncart;
     A.part_g = A.part_p + (size_t)nblk * 2 * b->nprim;
+    A.part_w = nmo > NMOMAX ? A.part_g + (size_t)nblk * NW * b->natom * 3 : nullptr;
     A.ntiles = ntiles;
     const size_t smem = sizeof(T) * (10 * KC * P + NMOMAX * KC + 2 * NMOMAX * P + 3 * KC * P);
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(adjoint_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e =
+            cudaFuncSetAttribute(adjoint_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(adjoint_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return cuda_status(e, "okg_rho_backward: smem attribute");
         configured = true;
     }
-    adjoint_kernel<T><<<nblk, NT, smem, st>>>(b->dev, g, A);
+    if (nmo > NMOMAX)
+        adjoint_kernel<T, true><<<nblk, NT, smem, st>>>(b->dev, g, A);
+    else
+        adjoint_kernel<T, false><<<nblk, NT, smem, st>>>(b->dev, g, A);
     long long n = (long long)nmo * b->ncart;
     reduce_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(A.part_c, n, nblk, 1, dC);
     n = 2ll * b->nprim;
@@ -413,7 +446,6 @@ extern "C" int okg_rho_backward(const okg_basis* b, const okg_grid* gr, int nmo,
 {
     if (!b || !gr || !d_coeff || !d_occ || !d_g_rho || !d_dcoeff || !d_dprim || !d_dgeo || !d_work || nmo <= 0)
         return set_error(OKG_ERR_ARG, "okg_rho_backward: NULL argument or nmo <= 0");
-    if (nmo > adj::NMOMAX) return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_backward: more than 48 MOs");
     if (precision != 32 && precision != 64) return set_error(OKG_ERR_ARG, "okg_rho_backward: precision 32 or 64");
     Grid g;
     g.x = gr->d_x;

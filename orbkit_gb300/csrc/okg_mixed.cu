@@ -157,6 +157,14 @@ __device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity)
     return false;
 }
 
+// Whether any thread of the CTA raised the abort flag, the same answer for every
+// lane of the calling warp (all 32 lanes must call it): decisions that lead to
+// warp-collective instructions (tcgen05.ld, shuffles) stay uniform.
+__device__ __forceinline__ bool warp_aborted(const int* flag)
+{
+    return __any_sync(0xffffffffu, *(const volatile int*)flag != 0);
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -617,8 +625,8 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int b = tbuf(ord);
-    if (*S.abort_flag) return -1;
-    if (!mbar_wait(S.bar_screened + 8 * b, tphase(ord), status, S.wait_limit)) {
+    if (warp_aborted(S.abort_flag)) return -1;
+    if (!__all_sync(0xffffffffu, mbar_wait(S.bar_screened + 8 * b, tphase(ord), status, S.wait_limit))) {
         *S.abort_flag = 1;
         return -1;
     }
@@ -798,7 +806,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
     if (!mbar_wait(S.bar_acc_full, accseq & 1u, status, S.wait_limit)) *S.abort_flag = 1;
     ++accseq;
     tc_fence_after();
-    if ((own[0] || own[1] || own[2] || own[3]) && !*S.abort_flag) {
+    if ((own[0] || own[1] || own[2] || own[3]) && !warp_aborted(S.abort_flag)) {
         const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
         const float2* occf = D.occf + pass * npad;
         const float2* occ2f = D.occf + (D.npass + pass) * npad;
@@ -819,9 +827,12 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
                 a3[i] = __uint_as_float(q[3][i]);
                 lo[i] = __uint_as_float(q[4][i]);
             }
+            // leading accumulators that no K-step of this job wrote hold another
+            // job's sums (or nothing yet): they count as zero
             if (nlead < 4) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
+                    a1[i] = nlead > 1 ? a1[i] : 0.f;
                     a2[i] = nlead > 2 ? a2[i] : 0.f;
                     a3[i] = 0.f;
                 }
@@ -881,7 +892,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
             const BasisDev& B = Dg.B;
             const unsigned char* nkeep = S.nkeep + tbuf(ord) * MAX_SHELLS;
-            while (c >= 0 && !*S.abort_flag) {
+            while (c >= 0 && !warp_aborted(S.abort_flag)) {
                 gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
                 ++nch;
                 nks += ksteps_of(km[c]);

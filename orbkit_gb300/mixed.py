@@ -201,21 +201,56 @@ class MixedEvaluator:
         g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
                         numpy.asarray(z, dtype=numpy.float64), is_vector, self.device)
         rho, grad = self.evaluate_device(g)
-        if out is not None:
+        if out is None:
+            # page-locked host arrays from torch's caching host allocator (reused
+            # after the first call): the read-back runs at pinned-copy bandwidth; the
+            # numpy arrays keep their tensors, and so the memory, alive
+            out = (torch.empty(rho.shape, dtype=torch.float64, pin_memory=True),
+                   torch.empty(grad.shape, dtype=torch.float64, pin_memory=True))
             out[0].copy_(rho, non_blocking=True)
             out[1].copy_(grad, non_blocking=True)
             torch.cuda.current_stream().synchronize()
-            return out
-        return rho.cpu().numpy(), grad.cpu().numpy()
+            return out[0].numpy(), out[1].numpy()
+        out[0].copy_(rho, non_blocking=True)
+        out[1].copy_(grad, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return out
 
     def check(self):
         self.plan.check()
 
 
+_evaluators = {}
+
+
+def evaluator_for(qc, cusp_radius=CUSP_RADIUS, device=None):
+    """A MixedEvaluator for this molecule, reused across calls: keyed by the basis and
+    geometry (the DeviceBasis fingerprint), the MO coefficients and occupations, the
+    cusp radius and the device, so that repeated drop-in calls (core.rho_compute with
+    precision='mixed') skip the plan set-up and the cusp-point search of a grid they
+    have seen (a few evaluators are kept)."""
+    import hashlib
+    import torch
+    from .basis import fingerprint, flatten
+    geo, ao_spec, mo_spec = unpack(qc)
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    h = hashlib.sha1(numpy.ascontiguousarray(mo_spec.get_coeffs(), dtype=numpy.float64).tobytes())
+    h.update(numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64).tobytes())
+    key = (fingerprint(geo, flatten(ao_spec)), h.hexdigest(), float(cusp_radius), str(dev))
+    ev = _evaluators.get(key)
+    if ev is None:
+        if len(_evaluators) >= 4:
+            _evaluators.pop(next(iter(_evaluators)))
+        ev = MixedEvaluator(qc, cusp_radius, dev)
+        _evaluators[key] = ev
+    return ev
+
+
 def rho_grad(qc, x, y, z, is_vector, cusp_radius=CUSP_RADIUS, return_device=False):
-    """rho and grad rho (3, npts) on the GPU mixed path, with the cusp region in FP64."""
+    """rho and grad rho (3, npts) on the GPU mixed path, with the cusp region in FP64
+    (evaluator and cusp points reused across calls on the same molecule and grid)."""
     from .core import _DeviceGrid
-    ev = MixedEvaluator(qc, cusp_radius)
+    ev = evaluator_for(qc, cusp_radius)
     if return_device:
         g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
                         numpy.asarray(z, dtype=numpy.float64), is_vector, ev.device)

@@ -79,6 +79,31 @@ def test_mixed_mid_full_grid_sampled(mixed):
     print("mid full grid, %d sampled points: %s" % (len(idx), rep))
 
 
+def test_mixed_kernel_deterministic(mixed):
+    """The tensor-core kernel gives the same bits on repeated launches over the whole
+    mid grid (tiles are handed out dynamically, so CTAs see different tiles each time;
+    every point's arithmetic must not depend on that)."""
+    import torch
+    from orbkit_gb300 import synthetic
+    from orbkit_gb300.core import _DeviceGrid
+    w = synthetic.mid()
+    ev = mixed.MixedEvaluator(w["qc"], cusp_radius=0.0)
+    g = _DeviceGrid(*w["grid"], False, ev.device)
+    n = g.npts
+    gd, keep = g.slice(0, n)
+    outs = []
+    for _ in range(3):
+        r = torch.full((n,), float("nan"), dtype=torch.float64, device=ev.device)
+        gr = torch.full((3, n), float("nan"), dtype=torch.float64, device=ev.device)
+        ev.plan.rho(gd, r, gr, n)
+        torch.cuda.synchronize()
+        ev.check()
+        outs.append((r.cpu().numpy(), gr.cpu().numpy()))
+    for r, gr in outs[1:]:
+        numpy.testing.assert_array_equal(r, outs[0][0])
+        numpy.testing.assert_array_equal(gr, outs[0][1])
+
+
 def test_mixed_spherical_fg(mixed):
     """Spherical basis with f and g shells and an 'N' factor (golden data of the reference)."""
     qc, d = load_golden("sph_fg_N.npz")
