@@ -599,23 +599,27 @@ def run_workload(args):
         mols = [(m["qc"], m["points"]) for m in d["molecules"]]
         npts = sum(pp.shape[1] for _, pp in mols)
         from orbkit_gb300 import mixed
-        ev = BatchEvaluator(mols, cusp_radius=0.0, tune=True)
+        # default: the cusp region (points within CUSP_RADIUS of a nucleus, a third of
+        # these atom-centred grids) keeps its steep primitives in FP64 inside the launch
+        ev = BatchEvaluator(mols, tune=True)
         graph = ev.capture()
         ms = _time_ms(graph.replay, args.steps, args.warmup)
         ev.check()
-        # the same batch with the points within CUSP_RADIUS of a nucleus recomputed by
-        # the FP64 path (a third of the points of these atom-centred grids)
-        ev.cusp_radius = mixed.CUSP_RADIUS
-        graph1 = ev.capture()
-        ms1 = _time_ms(graph1.replay, max(2, args.steps // 5), 1)
-        ev.check()
-        ncusp = sum(len(c[0]) for c in ev._cusp)
+        ncusp = int(sum(int((m["near"] >= 0).sum()) for m in ev.mols))
+        # the same batch from the tensor cores alone (no FP64 cusp part)
+        ev0 = BatchEvaluator(mols, cusp_radius=0.0, tune=True)
+        graph0 = ev0.capture()
+        ms0 = _time_ms(graph0.replay, args.steps, args.warmup)
+        ev0.check()
         out.update({"value": npts / (ms * 1e-3), "ms_per_step": ms,
                     "config": {"workload": "batch: 256 molecules, 3-60 atoms, atom-centred point sets",
                                "npts": npts, "molecules": len(mols), "tiles": ev.tiles(), "schedule": ev.schedule,
-                               "launch": "CUDA graph replay of one persistent kernel", "cusp_radius": 0.0,
-                               "with_fp64_cusp_points": {"cusp_radius": mixed.CUSP_RADIUS, "cusp_points": ncusp,
-                                                         "value": npts / (ms1 * 1e-3), "ms_per_step": ms1}}})
+                               "launch": "CUDA graph replay of one persistent kernel",
+                               "cusp": {"radius": ev.cusp_radius, "alpha_c": ev.cusp_alpha, "points": ncusp,
+                                        "mode": "steep primitives of the cusp atom in FP64 inside the launch"},
+                               "tensor_cores_alone": {"value": npts / (ms0 * 1e-3), "ms_per_step": ms0,
+                                                      "schedule": ev0.schedule},
+                               "with_over_without_cusp": ms0 / ms}})
     elif name == "ao":
         out.update(_ao_workload(args, flush, L))
     elif name == "overlap":

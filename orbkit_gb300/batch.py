@@ -4,11 +4,18 @@
 (tensor-core operand form), uploads its point set (3, n) and output buffers,
 and builds one okg_batch: all 128-point tiles of all molecules, handed out by a
 device counter to one persistent CTA per SM.  ``run()`` is a counter reset plus
-one kernel launch (plus the FP64 recomputation of cusp points when
-``cusp_radius > 0``); ``capture()`` records it in a CUDA graph; the schedule
+one kernel launch; ``capture()`` records it in a CUDA graph; the schedule
 (MMA N tile per MO pass, tiles per counter grab, molecule order, generation
 threads and points per thread) comes from the autotuner (orbkit_gb300.autotune),
 measured once per size bucket.
+
+The cusp region near nuclei stays FP64: by default (``cusp_mode='kernel'``) every
+point within ``cusp_radius`` of a nucleus has that atom's steep primitives (alpha >
+``cusp_alpha``, default mixed.cusp_alpha(cusp_radius)) evaluated, contracted with the
+MO coefficients and squared in FP64 inside the same persistent launch;
+``cusp_mode='recompute'`` instead recomputes those points whole with the FP64 path
+(exact FP64, but a third of an atom-centred grid lies in the cusp region);
+``cusp_radius=0`` evaluates every point on the tensor cores alone.
 """
 import ctypes
 
@@ -33,6 +40,7 @@ _SIGS = {
     "okg_batch_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "okg_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "okg_batch_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "okg_mixed_plan_set_cusp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double]),
 }
 
 N_TILES = (32, 64)
@@ -68,12 +76,19 @@ class _Plan:
 class BatchEvaluator:
     """molecules: sequence of (qc, points) with points a (3, n) float64 array."""
 
-    def __init__(self, molecules, want_grad=True, cusp_radius=0.0, tune=True, schedule=None, device=None):
+    def __init__(self, molecules, want_grad=True, cusp_radius=None, tune=True, schedule=None, device=None,
+                 cusp_mode="kernel", cusp_alpha=None):
         import torch
+        from . import mixed
         self._L = _L()
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.want_grad = want_grad
-        self.cusp_radius = cusp_radius
+        self.cusp_radius = mixed.CUSP_RADIUS if cusp_radius is None else cusp_radius
+        if cusp_mode not in ("kernel", "recompute"):
+            raise ValueError("cusp_mode must be 'kernel' or 'recompute'")
+        self.cusp_mode = cusp_mode
+        self.cusp_alpha = (mixed.cusp_alpha(self.cusp_radius) if self.cusp_radius > 0 else 0.0) \
+            if cusp_alpha is None else cusp_alpha
         self.mols = []
         for qc, pts in molecules:
             geo, ao_spec, mo_spec = unpack(qc)
@@ -86,6 +101,8 @@ class BatchEvaluator:
             m = {"basis": b, "C": C, "occ": occ, "pts": P, "n": n, "geo": numpy.asarray(geo, dtype=numpy.float64),
                  "rho": torch.empty(n, dtype=torch.float64, device=self.device),
                  "grad": torch.empty((3, n), dtype=torch.float64, device=self.device), "plans": {}}
+            m["near"] = mixed.near_atoms(m["geo"], P, self.cusp_radius, self.device) \
+                if self.kernel_cusp else None
             self.mols.append(m)
         self.npts = sum(m["n"] for m in self.mols)
         self._batch = None
@@ -94,10 +111,17 @@ class BatchEvaluator:
             schedule = self.autotune() if tune else {"n_max": 64, "grab": 1, "order": "given", "layout": (384, 1)}
         self.set_schedule(schedule)
 
+    @property
+    def kernel_cusp(self):
+        return self.cusp_mode == "kernel" and self.cusp_radius > 0
+
     # ------------------------------------------------------------- schedule
     def _plan(self, m, n_max):
         if n_max not in m["plans"]:
-            m["plans"][n_max] = _Plan(self._L, m["basis"], m["C"], m["occ"], n_max)
+            p = _Plan(self._L, m["basis"], m["C"], m["occ"], n_max)
+            if m["near"] is not None:
+                _lib.check(self._L.okg_mixed_plan_set_cusp(p.h, _lib.ptr(m["near"]), float(self.cusp_alpha)))
+            m["plans"][n_max] = p
         return m["plans"][n_max]
 
     def _order(self, order):
@@ -131,6 +155,8 @@ class BatchEvaluator:
         self._batch = h
         sms = __import__("torch").cuda.get_device_properties(self.device).multi_processor_count
         threads, points = sch.get("layout", (sch.get("threads", 384), 1))
+        if self.kernel_cusp and points != 1:
+            raise ValueError("the in-kernel FP64 cusp points need one point per generation thread")
         _lib.check(self._L.okg_batch_set_schedule(h, sch["grab"], sms, 384))
         _lib.check(self._L.okg_batch_set_generation(h, int(threads), int(points)))
         self.schedule = dict(sch)
@@ -145,8 +171,11 @@ class BatchEvaluator:
         key = "batch-" + autotune.bucket(nmol=len(self.mols), pts=self.npts,
                                          nao=max(m["basis"].ncart for m in self.mols),
                                          nmo=max(len(m["occ"]) for m in self.mols))
+        # (the FP64 cusp variant of the kernel has one point per generation thread)
+        layouts = [lt for lt in LAYOUTS if lt[1] == 1 or not self.kernel_cusp]
+        key += "-cusp" if self.kernel_cusp else ""
         cands = [{"n_max": n, "grab": g, "order": o, "layout": lt}
-                 for n in N_TILES for g in GRABS for o in ORDERS for lt in LAYOUTS]
+                 for n in N_TILES for g in GRABS for o in ORDERS for lt in layouts]
 
         def measure(c):
             self.set_schedule(c)
@@ -167,7 +196,7 @@ class BatchEvaluator:
     # ------------------------------------------------------------------ run
     def run(self, stream=None, cusp=True):
         _lib.check(self._L.okg_batch_run(self._batch, _lib.stream_handle(stream)))
-        if cusp and self.cusp_radius > 0:
+        if cusp and self.cusp_radius > 0 and self.cusp_mode == "recompute":
             self._fix_cusp()
 
     def _fix_cusp(self):

@@ -41,7 +41,8 @@ static int dfact(int n) { return n <= 0 ? 1 : n * dfact(n - 2); }
 // the mixed path.
 __global__ void prim_weights_kernel(const double* __restrict__ prim_in, const int* __restrict__ prim_L, int nprim,
                                     int is_normalized, double* __restrict__ prim_out, float* __restrict__ prim32,
-                                    PrimMx* __restrict__ prim_mx, double* __restrict__ prim_adj)
+                                    PrimMx* __restrict__ prim_mx, double* __restrict__ prim_adj,
+                                    double2* __restrict__ prim_cusp)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nprim) return;
@@ -71,24 +72,31 @@ __global__ void prim_weights_kernel(const double* __restrict__ prim_in, const in
     m.w = wh;
     m.wa = (float)(w * a);
     prim_mx[i] = m;
+    prim_cusp[i] = make_double2(a, w);
 }
 
 // Mixed path: order each shell's primitives by ascending exponent, so that a
 // tile keeps a prefix of them when screening (the radial sums do not depend on
 // the order).  One thread per shell, insertion sort (a handful of primitives).
-__global__ void sort_prim_mx_kernel(const Shell* __restrict__ shells, int nshell, PrimMx* __restrict__ prim_mx)
+// The FP64 {alpha, w} copy used for the cusp points of the mixed path is sorted
+// along (same permutation).
+__global__ void sort_prim_mx_kernel(const Shell* __restrict__ shells, int nshell, PrimMx* __restrict__ prim_mx,
+                                    double2* __restrict__ prim_cusp)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nshell) return;
     const int p0 = shells[s].prim0, np = shells[s].nprim;
     for (int i = 1; i < np; ++i) {
         const PrimMx v = prim_mx[p0 + i];
+        const double2 c = prim_cusp[p0 + i];
         int j = i - 1;
         while (j >= 0 && prim_mx[p0 + j].a2 > v.a2) {
             prim_mx[p0 + j + 1] = prim_mx[p0 + j];
+            prim_cusp[p0 + j + 1] = prim_cusp[p0 + j];
             --j;
         }
         prim_mx[p0 + j + 1] = v;
+        prim_cusp[p0 + j + 1] = c;
     }
 }
 
@@ -310,6 +318,9 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     const size_t o_scoef = lay.take(sizeof(double) * (sph_coef.size() + 1));
     const size_t o_chunks = lay.take(sizeof(int4) * chunks.size());
     const size_t o_pmx = lay.take(sizeof(PrimMx) * nprim);
+    const size_t o_pcusp = lay.take(sizeof(double2) * nprim);
+    const size_t o_asp = lay.take(sizeof(int) * (natom + 1));
+    const size_t o_ash = lay.take(sizeof(int) * nshell);
     const size_t o_padj = lay.take(sizeof(double) * 2 * nprim);
     const size_t o_mch = lay.take(sizeof(int4) * mchunks.size());
     const size_t o_mcc = lay.take(sizeof(int) * mcol_cart.size());
@@ -326,6 +337,17 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     if (e == cudaSuccess) e = cudaMemcpy(blk + o_primL, prim_L.data(), sizeof(int) * nprim, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_patom, prim_atom.data(), sizeof(int) * nprim, cudaMemcpyHostToDevice);
+    // shells of each atom (CSR), for the cusp points of the mixed path
+    std::vector<int> atom_shell_ptr(natom + 1, 0), atom_shells(nshell);
+    for (int s = 0; s < nshell; ++s) atom_shell_ptr[shells[s].atom + 1]++;
+    for (int a = 0; a < natom; ++a) atom_shell_ptr[a + 1] += atom_shell_ptr[a];
+    {
+        std::vector<int> fill(atom_shell_ptr.begin(), atom_shell_ptr.end() - 1);
+        for (int s = 0; s < nshell; ++s) atom_shells[fill[shells[s].atom]++] = s;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(blk + o_asp, atom_shell_ptr.data(), sizeof(int) * (natom + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(blk + o_ash, atom_shells.data(), sizeof(int) * nshell, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_crow, comp_row.data(), sizeof(int) * comp_row.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -364,6 +386,9 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     d.sph_coef = (const double*)(blk + o_scoef);
     d.chunks = (const int4*)(blk + o_chunks);
     d.prim_mx = (const PrimMx*)(blk + o_pmx);
+    d.prim_cusp = (const double2*)(blk + o_pcusp);
+    d.atom_shell_ptr = (const int*)(blk + o_asp);
+    d.atom_shells = (const int*)(blk + o_ash);
     d.prim_adj = (const double*)(blk + o_padj);
     d.mchunks = (const int4*)(blk + o_mch);
     d.mcol_cart = (const int*)(blk + o_mcc);
@@ -418,7 +443,9 @@ extern "C" int okg_basis_set_params(okg_basis* b, const double* d_geo, const dou
     atoms_kernel<<<(b->natom + 127) / 128, 128, 0, st>>>(d_geo, b->natom, (double*)b->dev.atoms);
     prim_weights_kernel<<<(b->nprim + 127) / 128, 128, 0, st>>>(d_prim, b->prim_L, b->nprim, b->is_normalized,
                                                                  (double*)b->dev.prim, (float*)b->dev.prim32,
-                                                                 (PrimMx*)b->dev.prim_mx, (double*)b->dev.prim_adj);
-    sort_prim_mx_kernel<<<(b->nshell + 127) / 128, 128, 0, st>>>(b->dev.shells, b->nshell, (PrimMx*)b->dev.prim_mx);
+                                                                 (PrimMx*)b->dev.prim_mx, (double*)b->dev.prim_adj,
+                                                                 (double2*)b->dev.prim_cusp);
+    sort_prim_mx_kernel<<<(b->nshell + 127) / 128, 128, 0, st>>>(b->dev.shells, b->nshell, (PrimMx*)b->dev.prim_mx,
+                                                                 (double2*)b->dev.prim_cusp);
     return cuda_status(cudaGetLastError(), "okg_basis_set_params");
 }

@@ -76,6 +76,9 @@ struct BasisDev {
     const int4* chunks;      // nchunk x {first shell, end shell, first Cartesian row, end row}
     const PrimMx* prim_mx;   // nprim (mixed path)
     const double* prim_adj;  // nprim x 2 : dw/dalpha, w/c (the alpha-dependent norm) for the adjoint
+    const double2* prim_cusp;  // nprim (mixed path): {alpha, w} in FP64, in the order of prim_mx (ascending alpha per shell)
+    const int* atom_shell_ptr; // natom + 1: shells of atom a are atom_shells[atom_shell_ptr[a] .. atom_shell_ptr[a+1])
+    const int* atom_shells;    // nshell
     const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= OKG_MKC columns)
     const int* mcol_cart;    // nmchunk x OKG_MKC: listed Cartesian row feeding each column, or -1
     const double* mcol_g;    // nmchunk x OKG_MKC: angular norm of each column (0 where unused)

@@ -299,6 +299,14 @@ struct alignas(16) MolDesc {
     int want_grad;
     int brick;           // regular grid covered by 4 x 4 x 8 bricks (else runs of 128 flattened points)
     int nby, nbz;        // bricks along y and z
+    // cusp points (null near: none): near[p] = the atom within whose cusp radius point p
+    // lies, or -1; there the atom's primitives with alpha > alpha_c are left out of the
+    // tensor-core operand and their part of every MO (C_eff in FP64, ceff) is added in
+    // FP64 in the epilogue
+    const short* near;
+    const double* ceff;  // nmo x ncart, FP64
+    double alpha_c;
+    double cusp_pad;
 };
 
 // Single-molecule launch.
@@ -456,10 +464,18 @@ struct TileFeed {
     int nmol, grab;
 };
 
-// Grid points of a generation thread: P consecutive rows of the tile.
+// Grid points of a generation thread: P consecutive rows of the tile, and the atom
+// whose cusp region holds each of them (-1: none).
 template <int P>
 struct GenPts {
     double x[P], y[P], z[P];
+    int near[P];
+};
+
+// The epilogue point of a generation thread (its TMEM lane): coordinates and cusp atom.
+struct EpiPt {
+    double x, y, z;
+    int near;
 };
 
 // Tile warp (the last warp of the CTA): takes tiles from the feed into buffer
@@ -619,9 +635,9 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
 // thread's store point (TMEM lane 32 (warp % 4) + lane of the epilogue) and its
 // generation points (rows P (tid % (128 / P)) + i).  Returns the tile (local to its
 // molecule) or -1 when there are no more.
-template <int P, bool BATCH>
+template <int P, bool BATCH, bool CUSP>
 __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t ord, long long& p, bool& valid,
-                                                   GenPts<P>& gp, int* status)
+                                                   GenPts<P>& gp, EpiPt& ep, int* status)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int b = tbuf(ord);
@@ -634,11 +650,19 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
     if (tile < 0) return -1;
     const MolDesc& D = S.mol[BATCH ? b : 0];
     valid = tile_point(D, tile, 32 * (warp & 3) + lane, p);
+    ep.near = -1;
+    if constexpr (CUSP) {
+        if (D.near && valid) ep.near = (int)__ldg(D.near + p);
+        if (ep.near >= D.B.natom) ep.near = -1;  // not an atom of the basis: no cusp treatment
+        if (ep.near >= 0) grid_point(D.g, p, ep.x, ep.y, ep.z);
+    }
 #pragma unroll
     for (int i = 0; i < P; ++i) {
         long long pg;
-        tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
+        const bool vg = tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
         grid_point(D.g, pg, gp.x[i], gp.y[i], gp.z[i]);
+        gp.near[i] = (CUSP && D.near && vg) ? (int)__ldg(D.near + pg) : -1;
+        if (gp.near[i] >= D.B.natom) gp.near[i] = -1;
     }
     return tile;
 }
@@ -702,10 +726,10 @@ __device__ __forceinline__ void shell_eval2_L(int L, const float (&X)[2], const 
 // chunk for this thread's P points and atoms, into the next stage of the ring.
 // With P = 2 the two points are adjacent in the M-major tile: each part of a
 // value pair is one packed conversion and one 4-byte store.
-template <int NTG, int P>
+template <int NTG, int P, bool CUSP>
 __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char* nkeep, int c, const CtaState& S,
                                           uint32_t& seq, AtomRun<P>& ar, unsigned chmask, const GenPts<P>& gp,
-                                          int* status)
+                                          double D_alpha_c2, int* status)
 {
     const int tid = threadIdx.x;
     const int r0 = P * (tid % (128 / P));  // first point row of this thread
@@ -733,9 +757,23 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
                 ar.Z[i] = dbl_to_flt_rn(Z);
             }
         }
+        // at a cusp point, the cusp atom's primitives with alpha > alpha_c (a sorted
+        // suffix of the kept ones) are left to the FP64 epilogue
+        int nkp[P];
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            nkp[i] = nk;
+            if (CUSP && gp.near[i] == sh.atom) {
+                const double a2c = D_alpha_c2;
+                int m = 0;
+                while (m < nk && B.prim_mx[sh.prim0 + m].a2 <= a2c) ++m;
+                nkp[i] = m;
+            }
+        }
         if constexpr (P == 1) {
             // primitives two at a time (two independent exponentials in flight)
             float R0 = 0.f, R1 = 0.f;
+            const int nk = nkp[0];
             for (int k = 0; k < nk; k += 2) {
                 const PrimMx pa = B.prim_mx[sh.prim0 + k];
                 const float ea = exp2_neg(pa.a2 * ar.rr[0]);
@@ -761,8 +799,8 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
             Radial<float> r[2] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
             for (int k = 0; k < nk; ++k) {
                 const PrimMx pm = B.prim_mx[sh.prim0 + k];
-                const float e0 = exp2_neg(pm.a2 * ar.rr[0]);
-                const float e1 = exp2_neg(pm.a2 * ar.rr[1]);
+                const float e0 = k < nkp[0] ? exp2_neg(pm.a2 * ar.rr[0]) : 0.f;
+                const float e1 = k < nkp[1] ? exp2_neg(pm.a2 * ar.rr[1]) : 0.f;
                 r[0].R0 = fmaf(pm.w, e0, r[0].R0);
                 r[0].R1 = fmaf(pm.wa, e0, r[0].R1);
                 r[1].R0 = fmaf(pm.w, e1, r[1].R0);
@@ -788,14 +826,54 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
     ++seq;
 }
 
+// FP64 part of the MO values (channel ch: 0 value, 1..3 d/dx, d/dy, d/dz) at a cusp
+// point that the tensor-core operand left out: for every shell of the cusp atom, its
+// primitives with alpha > alpha_c (orbkit's AO of orbkit/c_grid-based.c:38-71 restricted
+// to those primitives, exp in FP64), contracted with C_eff in FP64 for the MOs
+// [mo0, mo0 + 8).  Called by the lanes whose point is a cusp point only (not inlined:
+// its registers stay out of the epilogue's budget).
+__device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo0, int ch, double* out)
+{
+    const BasisDev& B = D.B;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = 0.0;
+    const int a = ep.near;
+    const double X = ep.x - __ldg(B.atoms + 4 * a), Y = ep.y - __ldg(B.atoms + 4 * a + 1),
+                 Z = ep.z - __ldg(B.atoms + 4 * a + 2);
+    const double rr = X * X + Y * Y + Z * Z;
+    const int t1 = __ldg(B.atom_shell_ptr + a + 1);
+    for (int t = __ldg(B.atom_shell_ptr + a); t < t1; ++t) {
+        const Shell sh = load_shell(B.shells + __ldg(B.atom_shells + t));
+        Radial<double> r{0.0, 0.0, 0.0};
+        bool any = false;
+        for (int q = 0; q < sh.nprim; ++q) {
+            const double2 pc = __ldg(B.prim_cusp + sh.prim0 + q);
+            if (pc.x <= D.alpha_c) continue;
+            const double e = pc.y * exp(-pc.x * rr);
+            r.R0 += e;
+            r.R1 += pc.x * e;
+            any = true;
+        }
+        if (!any) continue;
+        shell_eval_L(sh.L, X, Y, Z, r, 1u << ch, false, [&](int, int j, double v) {
+            const int row = __ldg(B.comp_row + sh.comp0 + j);
+            if (row < 0) return;
+            const double gv = v * __ldg(B.comp_g + sh.comp0 + j);
+            const double* cp = D.ceff + (long long)mo0 * B.ncart + sh.cart0 + row;
+            for (int i = 0; i < 8; ++i)
+                if (mo0 + i < D.nmo) out[i] += __ldg(cp + (long long)i * B.ncart) * gv;
+        });
+    }
+}
+
 // Generation threads: the epilogue of one job.  Warp w reads TMEM lanes
 // 32 (w % 4) .. (its 32 points) and owns the outputs o (0 = rho, 1..3 = d/dx,
 // d/dy, d/dz) with o % E == w / 4 (E = generation warps / 4); the 8-MO groups are reduced in double-float
 // FP32 (exact products by FMA, two-sum accumulation, about 44 bits) and added to
 // the FP64 accumulators.
-template <int E>
+template <int E, bool CUSP>
 __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nksteps, const CtaState& S,
-                                             uint32_t& accseq, double (&acc)[4], int* status)
+                                             uint32_t& accseq, double (&acc)[4], const EpiPt& ep, int* status)
 {
     const int warp = threadIdx.x >> 5;
     const int q = warp & 3, h = warp >> 2;
@@ -839,11 +917,25 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
             }
 #pragma unroll
             for (int i = 0; i < 8; ++i) v[i] = ((v[i] + a1[i]) + (a2[i] + a3[i])) + lo[i];
+            // a cusp point adds the FP64 part of its atom's steep primitives to every MO
+            // and forms its products in FP64 (the TMEM loads above and below stay
+            // outside this per-lane branch: they are warp-collective)
+            const bool cusp = CUSP && ep.near >= 0;
+            double cv[8];
+            if (cusp) cusp_part(D, ep, pass * npad + m0, 0, cv);
             if (own[0]) {
-                DF sr;
+                if (!cusp) {
+                    DF sr;
 #pragma unroll
-                for (int i = 0; i < 8; ++i) sr.add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
-                acc[0] += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
+                    for (int i = 0; i < 8; ++i) sr.add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
+                    acc[0] += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
+                } else {
+                    const double* oc = D.occ + pass * npad + m0;
+                    for (int i = 0; i < 8; ++i) {
+                        const double vf = (double)v[i] + cv[i];
+                        acc[0] += oc[i] * (vf * vf);
+                    }
+                }
             }
 #pragma unroll
             for (int o = 1; o < 4; ++o) {
@@ -854,10 +946,18 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
                 float vd[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) vd[i] = __uint_as_float(qd[0][i]);
-                DF sd;
+                if (!cusp) {
+                    DF sd;
 #pragma unroll
-                for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
-                acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
+                    for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
+                    acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
+                } else {
+                    double cd[8];
+                    cusp_part(D, ep, pass * npad + m0, o, cd);
+                    const double* oc2 = D.occ + (D.npass + pass) * npad + m0;
+                    for (int i = 0; i < 8; ++i)
+                        acc[o] += oc2[i] * (((double)v[i] + cv[i]) * ((double)vd[i] + cd[i]));
+                }
             }
         }
     }
@@ -869,7 +969,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
 // first chunk of the next job (screening its tile first when it starts one) is
 // generated before the epilogue of the current job, so the tensor core's tail
 // of a job overlaps useful work.
-template <int NTG, int P, bool BATCH>
+template <int NTG, int P, bool BATCH, bool CUSP>
 __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
 {
     constexpr int E = NTG / 128;  // epilogue warps per TMEM lane quarter
@@ -879,7 +979,8 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
     long long p = 0;
     bool valid = false;
     GenPts<P> gp;
-    if (gen_open_tile<P, BATCH>(S, ord, p, valid, gp, status) < 0) return;
+    EpiPt ep, ep_next;
+    if (gen_open_tile<P, BATCH, CUSP>(S, ord, p, valid, gp, ep, status) < 0) return;
     int gpass = 0;
     AtomRun<P> ar;
     int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
@@ -893,7 +994,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             const BasisDev& B = Dg.B;
             const unsigned char* nkeep = S.nkeep + tbuf(ord) * MAX_SHELLS;
             while (c >= 0 && !warp_aborted(S.abort_flag)) {
-                gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
+                gen_chunk<NTG, P, CUSP>(B, nkeep, c, S, seq, ar, chmask, gp, Dg.alpha_c * 1.4426950408889634, status);
                 ++nch;
                 nks += ksteps_of(km[c]);
                 c = next_kept(km, B.nmchunk, c);
@@ -912,7 +1013,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
         if (npass_next == Dg.npass) {
             ord_next = ord + 1;
             npass_next = 0;
-            more = gen_open_tile<P, BATCH>(S, ord_next, p_next, valid_next, gp, status) >= 0;
+            more = gen_open_tile<P, BATCH, CUSP>(S, ord_next, p_next, valid_next, gp, ep_next, status) >= 0;
         }
         int c_next = -1, nch_next = 0, nks_next = 0;
         if (more) {
@@ -921,15 +1022,15 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             ar = AtomRun<P>();
             c_next = next_kept(kmn, Dn.B.nmchunk, -1);
             if (c_next >= 0) {
-                gen_chunk<NTG, P>(Dn.B, S.nkeep + tbuf(ord_next) * MAX_SHELLS, c_next, S, seq, ar,
-                                  Dn.want_grad ? 0xFu : 0x1u, gp, status);
+                gen_chunk<NTG, P, CUSP>(Dn.B, S.nkeep + tbuf(ord_next) * MAX_SHELLS, c_next, S, seq, ar,
+                                  Dn.want_grad ? 0xFu : 0x1u, gp, Dn.alpha_c * 1.4426950408889634, status);
                 ++nch_next;
                 nks_next += ksteps_of(kmn[c_next]);
                 c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
             }
         }
         // the current job's epilogue (nothing to read if none of its chunks reached the tile)
-        if (nch > 0) gen_epilogue<E>(Dg, gpass, nks, S, accseq, acc, status);
+        if (nch > 0) gen_epilogue<E, CUSP>(Dg, gpass, nks, S, accseq, acc, ep, status);
         if (gpass == Dg.npass - 1) {
             if (valid && !*S.abort_flag) {
                 if (0 % E == h) Dg.rho[p] = acc[0];
@@ -946,6 +1047,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
         }
         if (!more) break;
         gpass = npass_next;
+        if (ord_next != ord) ep = ep_next;
         ord = ord_next;
         p = p_next;
         valid = valid_next;
@@ -1264,7 +1366,8 @@ inline void tiling(const Grid& g, MolDesc& D)
 
 // Descriptor of one molecule's call (host side).
 inline void make_desc(MolDesc& D, const BasisDev& B, const Grid& g, const void* bpack, const double* occ, int npass,
-                      int npad, int nmo, int want_grad, double* rho, double* grad, long long ld)
+                      int npad, int nmo, int want_grad, double* rho, double* grad, long long ld,
+                      const short* near = nullptr, const double* ceff = nullptr, double alpha_c = 0.0)
 {
     memset(&D, 0, sizeof(D));
     D.B = B;
@@ -1280,6 +1383,9 @@ inline void make_desc(MolDesc& D, const BasisDev& B, const Grid& g, const void* 
     D.npad = npad;
     D.nmo = nmo;
     D.want_grad = want_grad;
+    D.near = ceff ? near : nullptr;
+    D.ceff = ceff;
+    D.alpha_c = alpha_c;
     tiling(g, D);
 }
 
@@ -1289,7 +1395,7 @@ extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
 // Threads of a CTA: NTG generation threads, the MMA warp and the tile warp.
 __host__ __device__ constexpr int cta_threads(int ntg) { return ntg + 64; }
 
-template <int NTG, int PP>
+template <int NTG, int PP, bool CUSP>
 __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_kernel(const __grid_constant__ Params P)
 {
     __shared__ MolDesc mol[1];
@@ -1304,7 +1410,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_kernel(const __
     F.nmol = 1;
     F.grab = 1;
     if (threadIdx.x < NTG)
-        gen_role<NTG, PP, false>(S, P.status);
+        gen_role<NTG, PP, false, CUSP>(S, P.status);
     else if (threadIdx.x < NTG + 32)
         mma_role<false>(S, P.status);
     else
@@ -1326,7 +1432,7 @@ struct BatchParams {
     long long wait_limit;
 };
 
-template <int NTG, int PP>
+template <int NTG, int PP, bool CUSP>
 __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(const BatchParams P)
 {
     __shared__ MolDesc mol[NBUF];
@@ -1339,7 +1445,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(co
     F.nmol = P.nmol;
     F.grab = P.grab;
     if (threadIdx.x < NTG)
-        gen_role<NTG, PP, true>(S, P.status);
+        gen_role<NTG, PP, true, CUSP>(S, P.status);
     else if (threadIdx.x < NTG + 32)
         mma_role<true>(S, P.status);
     else
@@ -1420,9 +1526,19 @@ template <int NTG, int PP>
 static cudaError_t configure_one()
 {
     const int sm = (int)SMEM_BYTES;
-    cudaError_t e = cudaFuncSetAttribute(rho_mixed_kernel<NTG, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaError_t e =
+        cudaFuncSetAttribute(rho_mixed_kernel<NTG, PP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<NTG, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        e = cudaFuncSetAttribute(rho_mixed_batch_kernel<NTG, PP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 sm);
+    // the FP64 cusp variants exist for one point per generation thread
+    if constexpr (PP == 1) {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(rho_mixed_kernel<NTG, PP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(rho_mixed_batch_kernel<NTG, PP, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    }
     return e;
 }
 
@@ -1437,27 +1553,47 @@ static cudaError_t configure_kernels()
     return e;
 }
 
-static void launch_single(int layout, unsigned grid, cudaStream_t st, const Params& P)
+// cusp: the FP64 cusp variant (layouts with one point per generation thread only;
+// the callers check)
+static void launch_single(int layout, bool cusp, unsigned grid, cudaStream_t st, const Params& P)
 {
+    if (cusp) {
+        switch (layout) {
+        case 0: rho_mixed_kernel<256, 1, true><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+        case 2: rho_mixed_kernel<512, 1, true><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
+        default: rho_mixed_kernel<384, 1, true><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+        }
+        return;
+    }
     switch (layout) {
-    case 0: rho_mixed_kernel<256, 1><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
-    case 2: rho_mixed_kernel<512, 1><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
-    case 3: rho_mixed_kernel<256, 2><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
-    case 4: rho_mixed_kernel<384, 2><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
-    default: rho_mixed_kernel<384, 1><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+    case 0: rho_mixed_kernel<256, 1, false><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 2: rho_mixed_kernel<512, 1, false><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
+    case 3: rho_mixed_kernel<256, 2, false><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 4: rho_mixed_kernel<384, 2, false><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+    default: rho_mixed_kernel<384, 1, false><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
     }
 }
 
-static void launch_batch(int layout, unsigned grid, cudaStream_t st, const BatchParams& P)
+static void launch_batch(int layout, bool cusp, unsigned grid, cudaStream_t st, const BatchParams& P)
 {
+    if (cusp) {
+        switch (layout) {
+        case 0: rho_mixed_batch_kernel<256, 1, true><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+        case 2: rho_mixed_batch_kernel<512, 1, true><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
+        default: rho_mixed_batch_kernel<384, 1, true><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+        }
+        return;
+    }
     switch (layout) {
-    case 0: rho_mixed_batch_kernel<256, 1><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
-    case 2: rho_mixed_batch_kernel<512, 1><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
-    case 3: rho_mixed_batch_kernel<256, 2><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
-    case 4: rho_mixed_batch_kernel<384, 2><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
-    default: rho_mixed_batch_kernel<384, 1><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+    case 0: rho_mixed_batch_kernel<256, 1, false><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 2: rho_mixed_batch_kernel<512, 1, false><<<grid, cta_threads(512), SMEM_BYTES, st>>>(P); break;
+    case 3: rho_mixed_batch_kernel<256, 2, false><<<grid, cta_threads(256), SMEM_BYTES, st>>>(P); break;
+    case 4: rho_mixed_batch_kernel<384, 2, false><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
+    default: rho_mixed_batch_kernel<384, 1, false><<<grid, cta_threads(384), SMEM_BYTES, st>>>(P); break;
     }
 }
+
+inline bool layout_has_cusp(int layout) { return GEN_LAYOUTS[layout][1] == 1; }
 }  // namespace mx
 }  // namespace okg
 
@@ -1473,6 +1609,9 @@ struct okg_mixed_plan {
     size_t smem;
     int layout;  // index into GEN_LAYOUTS (generation threads, points per thread)
     long long wait_limit;  // polls per bounded device wait (WAIT_LIMIT by default)
+    double* ceff;          // C_eff in FP64 (nmo x ncart), for the cusp points
+    const short* near;     // caller's cusp-atom index per point, or null (no cusp treatment)
+    double alpha_c;        // primitives with alpha > alpha_c are FP64 at cusp points
 };
 
 extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_max, okg_mixed_plan** out);
@@ -1508,7 +1647,8 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->bpack_bytes = (size_t)p->npass * b->dev.nmchunk * 3 * p->npad * mx::ROWB;
     const size_t occ_off = (p->bpack_bytes + 255) & ~(size_t)255;
     const size_t st_off = occ_off + (((size_t)4 * p->npass * p->npad * 8 + 255) & ~(size_t)255);
-    cudaError_t e = cudaMalloc(&p->block, st_off + 256);
+    const size_t ceff_off = st_off + 256;
+    cudaError_t e = cudaMalloc(&p->block, ceff_off + (size_t)nmo * b->dev.ncart * sizeof(double));
     if (e != cudaSuccess) {
         free(p);
         return cuda_status(e, "okg_mixed_plan_create: cudaMalloc");
@@ -1516,6 +1656,9 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
     p->bpack = (__nv_bfloat16*)p->block;
     p->occ = (double*)((char*)p->block + occ_off);
     p->status = (int*)((char*)p->block + st_off);
+    p->ceff = (double*)((char*)p->block + ceff_off);
+    p->near = nullptr;
+    p->alpha_c = 0.0;
     cudaMemset(p->status, 0, sizeof(int));
     p->sm_count = sms;
     p->smem = mx::SMEM_BYTES;
@@ -1573,7 +1716,18 @@ extern "C" int okg_mixed_set_coeffs(okg_mixed_plan* p, const double* d_coeff, co
                                                        p->npad, p->bpack);
     const int total = p->npass * p->npad;
     mx::pack_occ_kernel<<<(total + 127) / 128, 128, 0, st>>>(d_occ, p->nmo, total, p->occ);
+    cudaError_t e = cudaMemcpyAsync(p->ceff, d_coeff, (size_t)p->nmo * B.ncart * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_status(e, "okg_mixed_set_coeffs: FP64 coefficient copy");
     return cuda_status(cudaGetLastError(), "okg_mixed_set_coeffs");
+}
+
+extern "C" int okg_mixed_plan_set_cusp(okg_mixed_plan* p, const int16_t* d_near, double alpha_c)
+{
+    if (!p || alpha_c < 0.0) return set_error(OKG_ERR_ARG, "okg_mixed_plan_set_cusp: NULL plan or alpha_c < 0");
+    p->near = (const short*)d_near;
+    p->alpha_c = alpha_c;
+    return OKG_OK;
 }
 
 extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_grad, double* d_rho, double* d_grad,
@@ -1597,7 +1751,8 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
     if (g.npts == 0) return OKG_OK;
     if (ld < g.npts) return set_error(OKG_ERR_ARG, "okg_rho_mixed: ld < npts");
     mx::Params P;
-    mx::make_desc(P.D, p->basis->dev, g, p->bpack, p->occ, p->npass, p->npad, p->nmo, want_grad, d_rho, d_grad, ld);
+    mx::make_desc(P.D, p->basis->dev, g, p->bpack, p->occ, p->npass, p->npad, p->nmo, want_grad, d_rho, d_grad, ld,
+                  p->near, p->ceff, p->alpha_c);
     P.status = p->status;
     P.counter = (unsigned long long*)((char*)p->status + 64);
     P.wait_limit = p->wait_limit;
@@ -1605,8 +1760,11 @@ extern "C" int okg_rho_mixed(okg_mixed_plan* p, const okg_grid* gr, int want_gra
         cudaError_t e0 = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), (cudaStream_t)stream);
         if (e0 != cudaSuccess) return cuda_status(e0, "okg_rho_mixed: counter reset");
     }
+    const bool cusp = P.D.near != nullptr;
+    if (cusp && !mx::layout_has_cusp(p->layout))
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed: the FP64 cusp points need one point per generation thread");
     const long long grid = P.D.ntiles < p->sm_count ? P.D.ntiles : p->sm_count;
-    mx::launch_single(p->layout, (unsigned)grid, (cudaStream_t)stream, P);
+    mx::launch_single(p->layout, cusp, (unsigned)grid, (cudaStream_t)stream, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed launch");
 }
 
@@ -1622,6 +1780,7 @@ struct okg_batch {
     int ctas;
     size_t smem;
     int layout;
+    bool cusp;  // some molecule's plan has FP64 cusp points
 };
 
 extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const okg_grid* grids, double* const* d_rho,
@@ -1633,6 +1792,7 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
     std::vector<mx::MolDesc> descs(nmol);
     long long tile0 = 0;
     int sms = 0;
+    bool any_cusp = false;
     for (int m = 0; m < nmol; ++m) {
         const okg_mixed_plan* p = plans[m];
         const okg_grid* gr = &grids[m];
@@ -1654,10 +1814,11 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
         g.nz = gr->nz;
         g.regular = gr->regular;
         mx::make_desc(D, p->basis->dev, g, p->bpack, p->occ, p->npass, p->npad, p->nmo, want_grad, d_rho[m],
-                      want_grad ? d_grad[m] : nullptr, ld[m]);
+                      want_grad ? d_grad[m] : nullptr, ld[m], p->near, p->ceff, p->alpha_c);
         D.tile0 = tile0;
         tile0 += D.ntiles;
         sms = p->sm_count;
+        any_cusp = any_cusp || D.near != nullptr;
     }
     okg_batch* b = (okg_batch*)calloc(1, sizeof(okg_batch));
     if (!b) return set_error(OKG_ERR_ALLOC, "okg_batch_create: host allocation");
@@ -1681,6 +1842,7 @@ extern "C" int okg_batch_create(int nmol, okg_mixed_plan* const* plans, const ok
     b->ctas = b->sm_count;
     b->smem = mx::SMEM_BYTES;
     b->layout = mx::LAYOUT_DEFAULT;
+    b->cusp = any_cusp;
     e = mx::configure_kernels();
     if (e != cudaSuccess) {
         cudaFree(b->block);
@@ -1743,8 +1905,10 @@ extern "C" int okg_batch_run(okg_batch* b, okg_stream stream)
     P.counter = b->d_counter;
     P.status = b->d_status;
     P.wait_limit = mx::WAIT_LIMIT;
+    if (b->cusp && !mx::layout_has_cusp(b->layout))
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_batch_run: the FP64 cusp points need one point per generation thread");
     const long long grid = b->total_tiles < b->ctas ? b->total_tiles : b->ctas;
-    mx::launch_batch(b->layout, (unsigned)grid, st, P);
+    mx::launch_batch(b->layout, b->cusp, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_batch_run launch");
 }
 
@@ -1909,6 +2073,6 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
     e = cudaMemsetAsync(P.counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return cuda_status(e, "okg_rho_mixed_noalloc: counter reset");
     const long long grid = P.D.ntiles < nd->sm_count ? P.D.ntiles : nd->sm_count;
-    launch_single(LAYOUT_DEFAULT, (unsigned)grid, st, P);
+    launch_single(LAYOUT_DEFAULT, false, (unsigned)grid, st, P);
     return cuda_status(cudaGetLastError(), "okg_rho_mixed_noalloc launch");
 }

@@ -22,6 +22,25 @@ MIXED_RHO_RTOL = 1e-6
 MIXED_RHO_FLOOR = 1e-10
 CUSP_RADIUS = 0.3
 
+
+def cusp_alpha(radius):
+    """Default exponent threshold of the in-kernel FP64 cusp treatment: primitives with
+    alpha > 24 ln 2 / r_c^2 fall below 2^-24 of their peak within the cusp radius r_c,
+    i.e. they vary on a scale finer than the cusp region."""
+    return 24.0 * numpy.log(2.0) / (radius * radius)
+
+
+def near_atoms(geo, pts, radius, device):
+    """int16 tensor (npts,) on the device: the atom within `radius` of each point
+    (3, npts) -- atoms are further apart than 2 radius -- or -1."""
+    import torch
+    P = torch.as_tensor(numpy.asarray(pts, dtype=numpy.float64), device=device)
+    G = torch.as_tensor(numpy.asarray(geo, dtype=numpy.float64).reshape(-1, 3), device=device)
+    near = torch.full((P.shape[1],), -1, dtype=torch.int16, device=device)
+    for a in range(G.shape[0]):
+        near[((P - G[a][:, None]) ** 2).sum(0) <= radius * radius] = a
+    return near
+
 _SIGS = {
     "okg_mixed_plan_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "okg_mixed_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -32,6 +51,7 @@ _SIGS = {
     "okg_mixed_plan_set_threads": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "okg_mixed_plan_set_generation": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "okg_mixed_plan_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
+    "okg_mixed_plan_set_cusp": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double]),
 }
 
 
@@ -73,6 +93,14 @@ class MixedPlan:
         """Generation threads per CTA and grid points per generation thread:
         (256|384|512, 1) or (256|384, 2)."""
         _lib.check(self._L.okg_mixed_plan_set_generation(self._h, int(threads), int(points_per_thread)))
+
+    def set_cusp(self, near, alpha_c):
+        """FP64 cusp points inside the tensor-core kernel: near (int16 device tensor, one
+        entry per point of the grids this plan evaluates, -1 = none) names each point's
+        cusp atom; that atom's primitives with alpha > alpha_c are evaluated in FP64 in
+        the epilogue.  near=None switches it off."""
+        self._near = near
+        _lib.check(self._L.okg_mixed_plan_set_cusp(self._h, _lib.ptr(near), float(alpha_c)))
 
     def set_wait_limit(self, polls):
         """Polls per bounded device wait (default 2^24); an expired wait makes check() raise."""
@@ -126,7 +154,11 @@ class MixedEvaluator:
     buffers.  ``update`` uploads new parameters from host arrays; ``evaluate``
     takes a host grid and writes host outputs."""
 
-    def __init__(self, qc, cusp_radius=CUSP_RADIUS, device=None):
+    def __init__(self, qc, cusp_radius=CUSP_RADIUS, device=None, cusp_mode="recompute", cusp_alpha_c=None):
+        """cusp_mode 'recompute' (default): the points within cusp_radius of a nucleus are
+        recomputed whole by the FP64 path after the tensor-core launch (exact FP64);
+        'kernel': the tensor-core kernel evaluates those points' steep primitives (alpha >
+        cusp_alpha_c, default cusp_alpha(cusp_radius)) in FP64 itself."""
         import torch
         geo, ao_spec, mo_spec = unpack(qc)
         self.device = device or torch.device("cuda", torch.cuda.current_device())
@@ -135,6 +167,11 @@ class MixedEvaluator:
         self.plan = MixedPlan(self.basis, mo_spec.get_coeffs(), occ)
         self.geo = numpy.asarray(geo, dtype=numpy.float64)
         self.cusp_radius = cusp_radius
+        if cusp_mode not in ("kernel", "recompute"):
+            raise ValueError("cusp_mode must be 'kernel' or 'recompute'")
+        self.cusp_mode = cusp_mode
+        self.cusp_alpha_c = cusp_alpha(cusp_radius) if (cusp_alpha_c is None and cusp_radius) else (cusp_alpha_c or 0.0)
+        self._near_key = None
         self._bufs = None
 
     def update(self, geo=None, prim=None, coeffs=None, occ=None, stream=None):
@@ -163,10 +200,33 @@ class MixedEvaluator:
             rho = torch.empty(n, dtype=torch.float64, device=self.device)
             grad = torch.empty((3, n), dtype=torch.float64, device=self.device)
         gd, keep = g.slice(0, n)
+        kernel_cusp = self.cusp_mode == "kernel" and self.cusp_radius and self.cusp_radius > 0
+        if kernel_cusp:
+            self._set_near(g)
         self.plan.rho(gd, rho, grad, n)
-        if self.cusp_radius and self.cusp_radius > 0:
+        if self.cusp_radius and self.cusp_radius > 0 and not kernel_cusp:
             self._cusp_fix(g, rho, grad)
         return rho, grad
+
+    def _set_near(self, g):
+        """Cusp atom of every point of g for the in-kernel FP64 cusp treatment (cached per grid)."""
+        import torch
+        key = (self.cusp_radius, self.geo.tobytes(),
+               tuple(numpy.ascontiguousarray(v).tobytes() for v in g.host) if g.regular else id(g))
+        if self._near_key != key:
+            self._near_grid = g
+            self._near_key = key
+            if g.regular:
+                near = torch.full((g.npts,), -1, dtype=torch.int16, device=self.device)
+                gx, gy, gz = g.host
+                nyz = len(gy) * len(gz)
+                for a, A in enumerate(self.geo):
+                    idx = cusp_points_regular(A[None, :], gx, gy, gz, self.cusp_radius)
+                    if len(idx):
+                        near[torch.from_numpy(idx).to(self.device)] = a
+            else:
+                near = near_atoms(self.geo, numpy.stack(g.host), self.cusp_radius, self.device)
+            self.plan.set_cusp(near, self.cusp_alpha_c)
 
     def _cusp_fix(self, g, rho, grad):
         import torch
