@@ -29,6 +29,9 @@ int set_error(int status, const char* msg)
 int cuda_status(cudaError_t e, const char* where)
 {
     if (e == cudaSuccess) return OKG_OK;
+    // consume the runtime's last-error state of this (non-sticky) error, so that a later
+    // cudaGetLastError() after a good launch does not report it again
+    (void)cudaGetLastError();
     std::string m = std::string(where) + ": " + cudaGetErrorString(e);
     g_last_error = m;
     return e == cudaErrorMemoryAllocation ? OKG_ERR_ALLOC : OKG_ERR_CUDA;

@@ -1389,7 +1389,10 @@ inline void make_desc(MolDesc& D, const BasisDev& B, const Grid& g, const void* 
     tiling(g, D);
 }
 
-extern __shared__ __align__(1024) unsigned char mx_smem_raw[];
+// Dynamic shared memory: aligned to 1024 bytes by hand (SMEM_BYTES holds the slack);
+// declaring it __align__(1024) would round the static part (the molecule descriptors)
+// up to a multiple of 1 KB and push the total past the 227 KB per-CTA limit.
+extern __shared__ __align__(16) unsigned char mx_smem_raw[];
 
 // Single molecule: its descriptor is copied to shared memory once.
 // Threads of a CTA: NTG generation threads, the MMA warp and the tile warp.
