@@ -34,7 +34,10 @@ def near_atoms(geo, pts, radius, device):
     """int16 tensor (npts,) on the device: the atom within `radius` of each point
     (3, npts) -- atoms are further apart than 2 radius -- or -1."""
     import torch
-    P = torch.as_tensor(numpy.asarray(pts, dtype=numpy.float64), device=device)
+    if isinstance(pts, torch.Tensor):
+        P = pts.to(device=device, dtype=torch.float64)
+    else:
+        P = torch.as_tensor(numpy.asarray(pts, dtype=numpy.float64), device=device)
     G = torch.as_tensor(numpy.asarray(geo, dtype=numpy.float64).reshape(-1, 3), device=device)
     near = torch.full((P.shape[1],), -1, dtype=torch.int16, device=device)
     for a in range(G.shape[0]):
