@@ -866,6 +866,70 @@ __device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo
     }
 }
 
+// The cusp atom's steep-primitive AO values at a cusp point, computed once per tile
+// (by the first epilogue that reaches the tile) and contracted per 8-MO group:
+// column (listed Cartesian row, -1 for none) and channel values (value, d/dx, d/dy,
+// d/dz) of up to MAX_SC canonical components; n = -1: more components than that (each
+// group then evaluates them again through cusp_part); n = -2: not prepared yet.
+constexpr int MAX_SC = 16;
+struct CuspVals {
+    int n;
+    int col[MAX_SC];
+    double v[MAX_SC][4];
+};
+
+__device__ __noinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, CuspVals& cz)
+{
+    const BasisDev& B = D.B;
+    cz.n = 0;
+    const int a = ep.near;
+    const double X = ep.x - __ldg(B.atoms + 4 * a), Y = ep.y - __ldg(B.atoms + 4 * a + 1),
+                 Z = ep.z - __ldg(B.atoms + 4 * a + 2);
+    const double rr = X * X + Y * Y + Z * Z;
+    const int t1 = __ldg(B.atom_shell_ptr + a + 1);
+    for (int t = __ldg(B.atom_shell_ptr + a); t < t1; ++t) {
+        const Shell sh = load_shell(B.shells + __ldg(B.atom_shells + t));
+        Radial<double> r{0.0, 0.0, 0.0};
+        bool any = false;
+        for (int q = 0; q < sh.nprim; ++q) {
+            const double2 pc = __ldg(B.prim_cusp + sh.prim0 + q);
+            if (pc.x <= D.alpha_c) continue;
+            const double e = pc.y * exp(-pc.x * rr);
+            r.R0 += e;
+            r.R1 += pc.x * e;
+            any = true;
+        }
+        if (!any) continue;
+        const int base = cz.n;
+        if (base + ncanon(sh.L) > MAX_SC) {
+            cz.n = -1;
+            return;
+        }
+        shell_eval_L(sh.L, X, Y, Z, r, 0xFu, false, [&](int ch, int j, double v) {
+            const int row = __ldg(B.comp_row + sh.comp0 + j);
+            cz.col[base + j] = row < 0 ? -1 : sh.cart0 + row;
+            cz.v[base + j][ch] = row < 0 ? 0.0 : v * __ldg(B.comp_g + sh.comp0 + j);
+        });
+        cz.n = base + ncanon(sh.L);
+    }
+}
+
+// out[i] = sum over the prepared components of C_eff[mo0 + i][col] x value (channel ch).
+__device__ __noinline__ void cusp_contract(const MolDesc& D, const CuspVals& cz, int mo0, int ch, double* out)
+{
+    const int ncart = D.B.ncart;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = 0.0;
+    for (int k = 0; k < cz.n; ++k) {
+        const int c = cz.col[k];
+        if (c < 0) continue;
+        const double gv = cz.v[k][ch];
+        const double* cp = D.ceff + (long long)mo0 * ncart + c;
+        for (int i = 0; i < 8; ++i)
+            if (mo0 + i < D.nmo) out[i] += __ldg(cp + (long long)i * ncart) * gv;
+    }
+}
+
 // Generation threads: the epilogue of one job.  Warp w reads TMEM lanes
 // 32 (w % 4) .. (its 32 points) and owns the outputs o (0 = rho, 1..3 = d/dx,
 // d/dy, d/dz) with o % E == w / 4 (E = generation warps / 4); the 8-MO groups are reduced in double-float
@@ -873,7 +937,8 @@ __device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo
 // the FP64 accumulators.
 template <int E, bool CUSP>
 __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nksteps, const CtaState& S,
-                                             uint32_t& accseq, double (&acc)[4], const EpiPt& ep, int* status)
+                                             uint32_t& accseq, double (&acc)[4], const EpiPt& ep, CuspVals& cz,
+                                             int* status)
 {
     const int warp = threadIdx.x >> 5;
     const int q = warp & 3, h = warp >> 2;
@@ -888,6 +953,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
         const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
         const float2* occf = D.occf + pass * npad;
         const float2* occ2f = D.occf + (D.npass + pass) * npad;
+        if (CUSP && ep.near >= 0 && cz.n == -2) cusp_prepare(D, ep, cz);
         const int nlead = nksteps < 4 ? nksteps : 4;  // leading accumulators written in this job
         int mo_end = D.nmo - pass * npad;
         mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
@@ -922,7 +988,12 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
             // outside this per-lane branch: they are warp-collective)
             const bool cusp = CUSP && ep.near >= 0;
             double cv[8];
-            if (cusp) cusp_part(D, ep, pass * npad + m0, 0, cv);
+            if (cusp) {
+                if (cz.n >= 0)
+                    cusp_contract(D, cz, pass * npad + m0, 0, cv);
+                else
+                    cusp_part(D, ep, pass * npad + m0, 0, cv);
+            }
             if (own[0]) {
                 if (!cusp) {
                     DF sr;
@@ -953,7 +1024,10 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
                     acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
                 } else {
                     double cd[8];
-                    cusp_part(D, ep, pass * npad + m0, o, cd);
+                    if (cz.n >= 0)
+                        cusp_contract(D, cz, pass * npad + m0, o, cd);
+                    else
+                        cusp_part(D, ep, pass * npad + m0, o, cd);
                     const double* oc2 = D.occ + (D.npass + pass) * npad + m0;
                     for (int i = 0; i < 8; ++i)
                         acc[o] += oc2[i] * (((double)v[i] + cv[i]) * ((double)vd[i] + cd[i]));
@@ -980,6 +1054,8 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
     bool valid = false;
     GenPts<P> gp;
     EpiPt ep, ep_next;
+    CuspVals cz;  // the current tile's steep AO values at this thread's cusp point
+    cz.n = -2;    // -2: not prepared for the current tile yet
     if (gen_open_tile<P, BATCH, CUSP>(S, ord, p, valid, gp, ep, status) < 0) return;
     int gpass = 0;
     AtomRun<P> ar;
@@ -1030,7 +1106,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             }
         }
         // the current job's epilogue (nothing to read if none of its chunks reached the tile)
-        if (nch > 0) gen_epilogue<E, CUSP>(Dg, gpass, nks, S, accseq, acc, ep, status);
+        if (nch > 0) gen_epilogue<E, CUSP>(Dg, gpass, nks, S, accseq, acc, ep, cz, status);
         if (gpass == Dg.npass - 1) {
             if (valid && !*S.abort_flag) {
                 if (0 % E == h) Dg.rho[p] = acc[0];
@@ -1047,7 +1123,10 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
         }
         if (!more) break;
         gpass = npass_next;
-        if (ord_next != ord) ep = ep_next;
+        if (ord_next != ord) {
+            ep = ep_next;
+            cz.n = -2;
+        }
         ord = ord_next;
         p = p_next;
         valid = valid_next;
