@@ -304,7 +304,7 @@ struct alignas(16) MolDesc {
     // tensor-core operand and their part of every MO (C_eff in FP64, ceff) is added in
     // FP64 in the epilogue
     const short* near;
-    const double* ceff;  // nmo x ncart, FP64
+    const double* ceff;  // C_eff transposed (ncart x nmo: the MOs of a column contiguous), FP64
     double alpha_c;
     double cusp_pad;
 };
@@ -832,6 +832,8 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
 // to those primitives, exp in FP64), contracted with C_eff in FP64 for the MOs
 // [mo0, mo0 + 8).  Called by the lanes whose point is a cusp point only (not inlined:
 // its registers stay out of the epilogue's budget).
+constexpr double CUSP_NEGLIGIBLE = 50.0;
+
 __device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo0, int ch, double* out)
 {
     const BasisDev& B = D.B;
@@ -848,7 +850,9 @@ __device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo
         bool any = false;
         for (int q = 0; q < sh.nprim; ++q) {
             const double2 pc = __ldg(B.prim_cusp + sh.prim0 + q);
-            if (pc.x <= D.alpha_c) continue;
+            // steep primitives only; one whose exponential is below e^-50 (2e-22) at the
+            // point adds nothing and is dropped
+            if (pc.x <= D.alpha_c || pc.x * rr > CUSP_NEGLIGIBLE) continue;
             const double e = pc.y * exp(-pc.x * rr);
             r.R0 += e;
             r.R1 += pc.x * e;
@@ -859,9 +863,9 @@ __device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo
             const int row = __ldg(B.comp_row + sh.comp0 + j);
             if (row < 0) return;
             const double gv = v * __ldg(B.comp_g + sh.comp0 + j);
-            const double* cp = D.ceff + (long long)mo0 * B.ncart + sh.cart0 + row;
+            const double* cp = D.ceff + (long long)(sh.cart0 + row) * D.nmo + mo0;
             for (int i = 0; i < 8; ++i)
-                if (mo0 + i < D.nmo) out[i] += __ldg(cp + (long long)i * B.ncart) * gv;
+                if (mo0 + i < D.nmo) out[i] += __ldg(cp + i) * gv;
         });
     }
 }
@@ -893,7 +897,9 @@ __device__ __noinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, Cus
         bool any = false;
         for (int q = 0; q < sh.nprim; ++q) {
             const double2 pc = __ldg(B.prim_cusp + sh.prim0 + q);
-            if (pc.x <= D.alpha_c) continue;
+            // steep primitives only; one whose exponential is below e^-50 (2e-22) at the
+            // point adds nothing and is dropped
+            if (pc.x <= D.alpha_c || pc.x * rr > CUSP_NEGLIGIBLE) continue;
             const double e = pc.y * exp(-pc.x * rr);
             r.R0 += e;
             r.R1 += pc.x * e;
@@ -917,16 +923,15 @@ __device__ __noinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, Cus
 // out[i] = sum over the prepared components of C_eff[mo0 + i][col] x value (channel ch).
 __device__ __noinline__ void cusp_contract(const MolDesc& D, const CuspVals& cz, int mo0, int ch, double* out)
 {
-    const int ncart = D.B.ncart;
 #pragma unroll
     for (int i = 0; i < 8; ++i) out[i] = 0.0;
     for (int k = 0; k < cz.n; ++k) {
         const int c = cz.col[k];
         if (c < 0) continue;
         const double gv = cz.v[k][ch];
-        const double* cp = D.ceff + (long long)mo0 * ncart + c;
+        const double* cp = D.ceff + (long long)c * D.nmo + mo0;  // 8 consecutive MOs of column c
         for (int i = 0; i < 8; ++i)
-            if (mo0 + i < D.nmo) out[i] += __ldg(cp + (long long)i * ncart) * gv;
+            if (mo0 + i < D.nmo) out[i] += __ldg(cp + i) * gv;
     }
 }
 
@@ -1566,6 +1571,16 @@ __global__ void pack_b_kernel(const double* __restrict__ C, int nmo, int ncart, 
     }
 }
 
+// C_eff (nmo x ncart) -> its transpose (ncart x nmo) for the FP64 cusp part.
+__global__ void transpose_kernel(const double* __restrict__ C, int nmo, int ncart, double* __restrict__ T)
+{
+    const long long n = (long long)nmo * ncart;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i / nmo), m = (int)(i - (long long)c * nmo);
+        T[i] = C[(long long)m * ncart + c];
+    }
+}
+
 // out[0 .. total): occupations (zero padded); out[total .. 2 total): twice them;
 // then the same 2 total values as double-float (hi, lo) pairs.
 __global__ void pack_occ_kernel(const double* __restrict__ occ, int nmo, int total, double* __restrict__ out)
@@ -1691,7 +1706,7 @@ struct okg_mixed_plan {
     size_t smem;
     int layout;  // index into GEN_LAYOUTS (generation threads, points per thread)
     long long wait_limit;  // polls per bounded device wait (WAIT_LIMIT by default)
-    double* ceff;          // C_eff in FP64 (nmo x ncart), for the cusp points
+    double* ceff;          // C_eff in FP64, transposed (ncart x nmo), for the cusp points
     const short* near;     // caller's cusp-atom index per point, or null (no cusp treatment)
     double alpha_c;        // primitives with alpha > alpha_c are FP64 at cusp points
 };
@@ -1798,9 +1813,7 @@ extern "C" int okg_mixed_set_coeffs(okg_mixed_plan* p, const double* d_coeff, co
                                                        p->npad, p->bpack);
     const int total = p->npass * p->npad;
     mx::pack_occ_kernel<<<(total + 127) / 128, 128, 0, st>>>(d_occ, p->nmo, total, p->occ);
-    cudaError_t e = cudaMemcpyAsync(p->ceff, d_coeff, (size_t)p->nmo * B.ncart * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) return cuda_status(e, "okg_mixed_set_coeffs: FP64 coefficient copy");
+    mx::transpose_kernel<<<p->sm_count * 4, 256, 0, st>>>(d_coeff, p->nmo, B.ncart, p->ceff);
     return cuda_status(cudaGetLastError(), "okg_mixed_set_coeffs");
 }
 
