@@ -196,10 +196,12 @@ int okg_mixed_plan_set_wait_limit(okg_mixed_plan* plan, long long polls);
 /* FP64 cusp region inside the tensor-core kernel (no counterpart in orbkit, which is
  * FP64 everywhere): d_near (device, one int16 per point of the grids later passed with
  * this plan -- the call's point index -- or NULL to switch off) names the atom within
- * whose cusp radius the point lies, or -1.  At such a point that atom's primitives with
- * alpha > alpha_c are left out of the BF16 operand; the epilogue evaluates them in FP64
- * (exp, radial sums, polynomials), contracts them with C_eff in FP64 and forms the
- * point's density products in FP64.  The plan keeps the pointer (the caller keeps the
+ * whose cusp radius the point lies, or -1.  In every 128-point tile that holds such a
+ * point, the primitives with alpha > alpha_c of the atoms named there are left out of
+ * the BF16 operand; the epilogue evaluates them in FP64 at each point of the tile (exp,
+ * radial sums, polynomials; those below e^-50 at the point dropped), contracts them with
+ * C_eff in FP64 and forms the point's density products in FP64.  More than 8 such atoms
+ * in one tile is reported by okg_mixed_status / okg_batch_status as OKG_ERR_UNSUPPORTED.  The plan keeps the pointer (the caller keeps the
  * array alive); a batch takes the setting of each molecule's plan at okg_batch_create. */
 int okg_mixed_plan_set_cusp(okg_mixed_plan* plan, const int16_t* d_near, double alpha_c);
 

@@ -342,12 +342,16 @@ struct CtaState {
     unsigned char* nkeep;        // NBUF x MAX_SHELLS: per shell, kept primitives | owning generation group << 5
     unsigned* kmask;             // NBUF x MAX_CHUNKS: per chunk, columns whose shell is kept for the buffer's tile
     long long* tile_slot;        // NBUF: tile of the buffer (local to its molecule); -1: no more tiles
+    int* cusp_atoms;             // NBUF x (1 + NCA): count, then the atoms whose cusp region holds a point of the tile
     MolDesc* mol;                // NBUF: molecule of the buffer's tile (one copy for the single-molecule kernel)
 };
 
 // Per-tile screening tables live in shared memory: at most MAX_SHELLS shells and
 // MAX_CHUNKS chunks per molecule on the mixed path.
 constexpr int MAX_SHELLS = 2048;
+// FP64 cusp region: at most NCA atoms whose cusp region holds a point of one tile (more
+// raise status bit 2, reported as OKG_ERR_UNSUPPORTED; the first NCA are treated)
+constexpr int NCA = 8;
 constexpr int MAX_CHUNKS = 192;
 // Tile buffers (index, descriptor, screening tables) between the tile warp and the
 // generation threads / MMA warp: the tile warp screens up to NBUF - 1 tiles ahead.
@@ -464,18 +468,19 @@ struct TileFeed {
     int nmol, grab;
 };
 
-// Grid points of a generation thread: P consecutive rows of the tile, and the atom
-// whose cusp region holds each of them (-1: none).
+// Grid points of a generation thread: P consecutive rows of the tile.
 template <int P>
 struct GenPts {
     double x[P], y[P], z[P];
-    int near[P];
 };
 
-// The epilogue point of a generation thread (its TMEM lane): coordinates and cusp atom.
+// The epilogue point of a generation thread (its TMEM lane): coordinates, and the
+// cusp atoms of its tile (ncusp of them; the list is copied out of the tile buffer,
+// which the tile warp may reuse before the epilogue runs).
 struct EpiPt {
     double x, y, z;
-    int near;
+    int ncusp;
+    int atoms[NCA];
 };
 
 // Tile warp (the last warp of the CTA): takes tiles from the feed into buffer
@@ -485,7 +490,7 @@ struct EpiPt {
 // kept shells to generation groups, then arrives on the buffer's "screened"
 // barrier.  It runs up to NBUF - 1 tiles ahead of the generation threads, so none
 // of this is on their path.  A buffer with tile -1 ends the CTA.
-template <int NG, bool BATCH>
+template <int NG, bool BATCH, bool CUSP>
 __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, int* status)
 {
     static_assert(NG >= 1 && NG <= (256 >> KEEP_BITS), "generation group index must fit the screening byte");
@@ -566,6 +571,40 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
         unsigned* km = S.kmask + b * MAX_CHUNKS;
         unsigned char* nkeep = S.nkeep + b * MAX_SHELLS;
         for (int c = lane; c < B.nmchunk; c += 32) km[c] = 0u;
+        // the atoms whose cusp region holds a point of the tile (the caller's per-point
+        // table), at most NCA; their steep primitives leave the tile's BF16 operand
+        int* ca = S.cusp_atoms + b * (1 + NCA);
+        int nca = 0;
+        int cat[NCA];
+        if (CUSP && D.near) {
+            int mine[M / 32];
+#pragma unroll
+            for (int i = 0; i < M / 32; ++i) {
+                long long pg;
+                mine[i] = tile_point(D, t, lane + 32 * i, pg) ? (int)__ldg(D.near + pg) : -1;
+                if (mine[i] >= B.natom) mine[i] = -1;
+            }
+            for (;;) {
+                int cand = -1;
+#pragma unroll
+                for (int i = 0; i < M / 32; ++i) cand = mine[i] >= 0 ? mine[i] : cand;
+                const unsigned any = __ballot_sync(0xffffffffu, cand >= 0);
+                if (!any) break;
+                const int a = __shfl_sync(0xffffffffu, cand, __ffs(any) - 1);
+                if (nca == NCA) {
+                    if (lane == 0) atomicOr(status, 2);
+                    break;
+                }
+                cat[nca++] = a;
+#pragma unroll
+                for (int i = 0; i < M / 32; ++i) mine[i] = mine[i] == a ? -1 : mine[i];
+            }
+        }
+        if (lane == 0) {
+            ca[0] = nca;
+            for (int i = 0; i < nca; ++i) ca[1 + i] = cat[i];
+        }
+        const double a2c = D.alpha_c * 1.4426950408889634;
         __syncwarp();
         // a primitive is kept while alpha log2(e) d^2 <= SCREEN_LOG2 (primitives sorted by alpha per shell)
         for (int si = lane; si < B.nshell; si += 32) {
@@ -578,6 +617,17 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
             const float d2 = dx * dx + dy * dy + dz * dz;
             int nk = 0;
             while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+            if (CUSP) {
+                // a cusp atom of the tile keeps only its smooth primitives (alpha <= alpha_c, a
+                // prefix): the epilogue adds the steep ones in FP64 at every point of the tile
+                bool cusp_atom = false;
+                for (int i = 0; i < nca; ++i) cusp_atom = cusp_atom || cat[i] == sh.atom;
+                if (cusp_atom) {
+                    int m = 0;
+                    while (m < nk && B.prim_mx[sh.prim0 + m].a2 <= a2c) ++m;
+                    nk = m;
+                }
+            }
             nkeep[si] = (unsigned char)nk;
             if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
         }
@@ -650,19 +700,18 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
     if (tile < 0) return -1;
     const MolDesc& D = S.mol[BATCH ? b : 0];
     valid = tile_point(D, tile, 32 * (warp & 3) + lane, p);
-    ep.near = -1;
+    ep.ncusp = 0;
     if constexpr (CUSP) {
-        if (D.near && valid) ep.near = (int)__ldg(D.near + p);
-        if (ep.near >= D.B.natom) ep.near = -1;  // not an atom of the basis: no cusp treatment
-        if (ep.near >= 0) grid_point(D.g, p, ep.x, ep.y, ep.z);
+        const int* ca = S.cusp_atoms + b * (1 + NCA);
+        ep.ncusp = valid ? ca[0] : 0;
+        for (int i = 0; i < ep.ncusp; ++i) ep.atoms[i] = ca[1 + i];
+        if (ep.ncusp > 0) grid_point(D.g, p, ep.x, ep.y, ep.z);
     }
 #pragma unroll
     for (int i = 0; i < P; ++i) {
         long long pg;
-        const bool vg = tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
+        tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
         grid_point(D.g, pg, gp.x[i], gp.y[i], gp.z[i]);
-        gp.near[i] = (CUSP && D.near && vg) ? (int)__ldg(D.near + pg) : -1;
-        if (gp.near[i] >= D.B.natom) gp.near[i] = -1;
     }
     return tile;
 }
@@ -726,10 +775,10 @@ __device__ __forceinline__ void shell_eval2_L(int L, const float (&X)[2], const 
 // chunk for this thread's P points and atoms, into the next stage of the ring.
 // With P = 2 the two points are adjacent in the M-major tile: each part of a
 // value pair is one packed conversion and one 4-byte store.
-template <int NTG, int P, bool CUSP>
+template <int NTG, int P>
 __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char* nkeep, int c, const CtaState& S,
                                           uint32_t& seq, AtomRun<P>& ar, unsigned chmask, const GenPts<P>& gp,
-                                          double D_alpha_c2, int* status)
+                                          int* status)
 {
     const int tid = threadIdx.x;
     const int r0 = P * (tid % (128 / P));  // first point row of this thread
@@ -757,23 +806,9 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
                 ar.Z[i] = dbl_to_flt_rn(Z);
             }
         }
-        // at a cusp point, the cusp atom's primitives with alpha > alpha_c (a sorted
-        // suffix of the kept ones) are left to the FP64 epilogue
-        int nkp[P];
-#pragma unroll
-        for (int i = 0; i < P; ++i) {
-            nkp[i] = nk;
-            if (CUSP && gp.near[i] == sh.atom) {
-                const double a2c = D_alpha_c2;
-                int m = 0;
-                while (m < nk && B.prim_mx[sh.prim0 + m].a2 <= a2c) ++m;
-                nkp[i] = m;
-            }
-        }
         if constexpr (P == 1) {
             // primitives two at a time (two independent exponentials in flight)
             float R0 = 0.f, R1 = 0.f;
-            const int nk = nkp[0];
             for (int k = 0; k < nk; k += 2) {
                 const PrimMx pa = B.prim_mx[sh.prim0 + k];
                 const float ea = exp2_neg(pa.a2 * ar.rr[0]);
@@ -799,8 +834,8 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
             Radial<float> r[2] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
             for (int k = 0; k < nk; ++k) {
                 const PrimMx pm = B.prim_mx[sh.prim0 + k];
-                const float e0 = k < nkp[0] ? exp2_neg(pm.a2 * ar.rr[0]) : 0.f;
-                const float e1 = k < nkp[1] ? exp2_neg(pm.a2 * ar.rr[1]) : 0.f;
+                const float e0 = exp2_neg(pm.a2 * ar.rr[0]);
+                const float e1 = exp2_neg(pm.a2 * ar.rr[1]);
                 r[0].R0 = fmaf(pm.w, e0, r[0].R0);
                 r[0].R1 = fmaf(pm.wa, e0, r[0].R1);
                 r[1].R0 = fmaf(pm.w, e1, r[1].R0);
@@ -834,15 +869,14 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
 // its registers stay out of the epilogue's budget).
 constexpr double CUSP_NEGLIGIBLE = 50.0;
 
-__device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo0, int ch, double* out)
+// The steep primitives of one cusp atom at the point (X, Y, Z from the nucleus):
+// for every shell of the atom with a steep primitive that is not negligible there,
+// visit(shell, radial sums) -- FP64 exp, orbkit's AO of orbkit/c_grid-based.c:38-71
+// restricted to those primitives.
+template <typename Visit>
+__device__ __forceinline__ void steep_shells(const MolDesc& D, int a, double rr, Visit&& visit)
 {
     const BasisDev& B = D.B;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) out[i] = 0.0;
-    const int a = ep.near;
-    const double X = ep.x - __ldg(B.atoms + 4 * a), Y = ep.y - __ldg(B.atoms + 4 * a + 1),
-                 Z = ep.z - __ldg(B.atoms + 4 * a + 2);
-    const double rr = X * X + Y * Y + Z * Z;
     const int t1 = __ldg(B.atom_shell_ptr + a + 1);
     for (int t = __ldg(B.atom_shell_ptr + a); t < t1; ++t) {
         const Shell sh = load_shell(B.shells + __ldg(B.atom_shells + t));
@@ -858,23 +892,44 @@ __device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo
             r.R1 += pc.x * e;
             any = true;
         }
-        if (!any) continue;
-        shell_eval_L(sh.L, X, Y, Z, r, 1u << ch, false, [&](int, int j, double v) {
-            const int row = __ldg(B.comp_row + sh.comp0 + j);
-            if (row < 0) return;
-            const double gv = v * __ldg(B.comp_g + sh.comp0 + j);
-            const double* cp = D.ceff + (long long)(sh.cart0 + row) * D.nmo + mo0;
-            for (int i = 0; i < 8; ++i)
-                if (mo0 + i < D.nmo) out[i] += __ldg(cp + i) * gv;
+        if (any && !visit(sh, r)) return;
+    }
+}
+
+// FP64 part of the MO values (channel ch: 0 value, 1..3 d/dx, d/dy, d/dz) that the
+// tensor-core operand left out at a point of a cusp tile: the steep primitives of the
+// tile's cusp atoms, contracted with C_eff in FP64 for the MOs [mo0, mo0 + 8).  Used when
+// the point has more steep components than a CuspVals holds (not inlined: its
+// registers stay out of the epilogue's budget).
+__device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo0, int ch, double* out)
+{
+    const BasisDev& B = D.B;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = 0.0;
+    for (int ia = 0; ia < ep.ncusp; ++ia) {
+        const int a = ep.atoms[ia];
+        const double X = ep.x - __ldg(B.atoms + 4 * a), Y = ep.y - __ldg(B.atoms + 4 * a + 1),
+                     Z = ep.z - __ldg(B.atoms + 4 * a + 2);
+        steep_shells(D, a, X * X + Y * Y + Z * Z, [&](const Shell& sh, const Radial<double>& r) {
+            shell_eval_L(sh.L, X, Y, Z, r, 1u << ch, false, [&](int, int j, double v) {
+                const int row = __ldg(B.comp_row + sh.comp0 + j);
+                if (row < 0) return;
+                const double gv = v * __ldg(B.comp_g + sh.comp0 + j);
+                const double* cp = D.ceff + (long long)(sh.cart0 + row) * D.nmo + mo0;
+                for (int i = 0; i < 8; ++i)
+                    if (mo0 + i < D.nmo) out[i] += __ldg(cp + i) * gv;
+            });
+            return true;
         });
     }
 }
 
-// The cusp atom's steep-primitive AO values at a cusp point, computed once per tile
-// (by the first epilogue that reaches the tile) and contracted per 8-MO group:
-// column (listed Cartesian row, -1 for none) and channel values (value, d/dx, d/dy,
-// d/dz) of up to MAX_SC canonical components; n = -1: more components than that (each
-// group then evaluates them again through cusp_part); n = -2: not prepared yet.
+// The steep AO values of the tile's cusp atoms at this point, computed once per tile
+// (by the first epilogue that reaches the tile) and contracted per 8-MO group: column
+// (listed Cartesian row, -1 for none) and channel values (value, d/dx, d/dy, d/dz) of up
+// to MAX_SC canonical components; n = 0: nothing steep is left at the point (the
+// density products stay on the double-float path); n = -1: more components than that
+// (each group then evaluates them again through cusp_part); n = -2: not prepared yet.
 constexpr int MAX_SC = 16;
 struct CuspVals {
     int n;
@@ -886,37 +941,24 @@ __device__ __noinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, Cus
 {
     const BasisDev& B = D.B;
     cz.n = 0;
-    const int a = ep.near;
-    const double X = ep.x - __ldg(B.atoms + 4 * a), Y = ep.y - __ldg(B.atoms + 4 * a + 1),
-                 Z = ep.z - __ldg(B.atoms + 4 * a + 2);
-    const double rr = X * X + Y * Y + Z * Z;
-    const int t1 = __ldg(B.atom_shell_ptr + a + 1);
-    for (int t = __ldg(B.atom_shell_ptr + a); t < t1; ++t) {
-        const Shell sh = load_shell(B.shells + __ldg(B.atom_shells + t));
-        Radial<double> r{0.0, 0.0, 0.0};
-        bool any = false;
-        for (int q = 0; q < sh.nprim; ++q) {
-            const double2 pc = __ldg(B.prim_cusp + sh.prim0 + q);
-            // steep primitives only; one whose exponential is below e^-50 (2e-22) at the
-            // point adds nothing and is dropped
-            if (pc.x <= D.alpha_c || pc.x * rr > CUSP_NEGLIGIBLE) continue;
-            const double e = pc.y * exp(-pc.x * rr);
-            r.R0 += e;
-            r.R1 += pc.x * e;
-            any = true;
-        }
-        if (!any) continue;
-        const int base = cz.n;
-        if (base + ncanon(sh.L) > MAX_SC) {
-            cz.n = -1;
-            return;
-        }
-        shell_eval_L(sh.L, X, Y, Z, r, 0xFu, false, [&](int ch, int j, double v) {
-            const int row = __ldg(B.comp_row + sh.comp0 + j);
-            cz.col[base + j] = row < 0 ? -1 : sh.cart0 + row;
-            cz.v[base + j][ch] = row < 0 ? 0.0 : v * __ldg(B.comp_g + sh.comp0 + j);
+    for (int ia = 0; ia < ep.ncusp && cz.n >= 0; ++ia) {
+        const int a = ep.atoms[ia];
+        const double X = ep.x - __ldg(B.atoms + 4 * a), Y = ep.y - __ldg(B.atoms + 4 * a + 1),
+                     Z = ep.z - __ldg(B.atoms + 4 * a + 2);
+        steep_shells(D, a, X * X + Y * Y + Z * Z, [&](const Shell& sh, const Radial<double>& r) {
+            const int base = cz.n;
+            if (base + ncanon(sh.L) > MAX_SC) {
+                cz.n = -1;
+                return false;
+            }
+            shell_eval_L(sh.L, X, Y, Z, r, 0xFu, false, [&](int ch, int j, double v) {
+                const int row = __ldg(B.comp_row + sh.comp0 + j);
+                cz.col[base + j] = row < 0 ? -1 : sh.cart0 + row;
+                cz.v[base + j][ch] = row < 0 ? 0.0 : v * __ldg(B.comp_g + sh.comp0 + j);
+            });
+            cz.n = base + ncanon(sh.L);
+            return true;
         });
-        cz.n = base + ncanon(sh.L);
     }
 }
 
@@ -958,7 +1000,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
         const uint32_t tl = S.tmem + ((uint32_t)(32 * q) << 16);
         const float2* occf = D.occf + pass * npad;
         const float2* occ2f = D.occf + (D.npass + pass) * npad;
-        if (CUSP && ep.near >= 0 && cz.n == -2) cusp_prepare(D, ep, cz);
+        if (CUSP && ep.ncusp > 0 && cz.n == -2) cusp_prepare(D, ep, cz);
         const int nlead = nksteps < 4 ? nksteps : 4;  // leading accumulators written in this job
         int mo_end = D.nmo - pass * npad;
         mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
@@ -991,7 +1033,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
             // a cusp point adds the FP64 part of its atom's steep primitives to every MO
             // and forms its products in FP64 (the TMEM loads above and below stay
             // outside this per-lane branch: they are warp-collective)
-            const bool cusp = CUSP && ep.near >= 0;
+            const bool cusp = CUSP && ep.ncusp > 0 && cz.n != 0;
             double cv[8];
             if (cusp) {
                 if (cz.n >= 0)
@@ -1075,7 +1117,7 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             const BasisDev& B = Dg.B;
             const unsigned char* nkeep = S.nkeep + tbuf(ord) * MAX_SHELLS;
             while (c >= 0 && !warp_aborted(S.abort_flag)) {
-                gen_chunk<NTG, P, CUSP>(B, nkeep, c, S, seq, ar, chmask, gp, Dg.alpha_c * 1.4426950408889634, status);
+                gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
                 ++nch;
                 nks += ksteps_of(km[c]);
                 c = next_kept(km, B.nmchunk, c);
@@ -1103,8 +1145,8 @@ __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
             ar = AtomRun<P>();
             c_next = next_kept(kmn, Dn.B.nmchunk, -1);
             if (c_next >= 0) {
-                gen_chunk<NTG, P, CUSP>(Dn.B, S.nkeep + tbuf(ord_next) * MAX_SHELLS, c_next, S, seq, ar,
-                                  Dn.want_grad ? 0xFu : 0x1u, gp, Dn.alpha_c * 1.4426950408889634, status);
+                gen_chunk<NTG, P>(Dn.B, S.nkeep + tbuf(ord_next) * MAX_SHELLS, c_next, S, seq, ar,
+                                  Dn.want_grad ? 0xFu : 0x1u, gp, status);
                 ++nch_next;
                 nks_next += ksteps_of(kmn[c_next]);
                 c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
@@ -1371,6 +1413,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
     uint32_t* tmem_slot = (uint32_t*)(S.tile_slot + NBUF);
     S.abort_flag = (int*)(tmem_slot + 1);
     S.nkeep = (unsigned char*)(S.abort_flag + 1);
+    S.cusp_atoms = (int*)(S.nkeep + NBUF * MAX_SHELLS);
     S.mol = mol;
     S.bar_full = smem_u32(bar);
     S.bar_empty = smem_u32(bar + 2);
@@ -1413,7 +1456,7 @@ __device__ __forceinline__ CtaState cta_setup(unsigned char* smem, MolDesc* mol,
 
 // bytes of dynamic shared memory of the mixed kernels (1 KB alignment slack included)
 constexpr size_t SMEM_BYTES = 1024 + NSTAGE * (A_STAGE + B_STAGE) + 4 * NBUF * MAX_CHUNKS + (9 + 2 * NBUF) * 8 +
-                              NBUF * 8 + 4 + 4 + NBUF * MAX_SHELLS + 64;
+                              NBUF * 8 + 4 + 4 + NBUF * MAX_SHELLS + NBUF * (1 + NCA) * 4 + 64;
 static_assert(SMEM_BYTES + NBUF * sizeof(MolDesc) <= 232448, "mixed kernel shared memory above the 227 KB per-CTA limit");
 static_assert(KC == 32, "column masks are 32-bit and operand rows one 64-byte swizzle row");
 static_assert(sizeof(MolDesc) % 16 == 0, "descriptors are copied in 16-byte units");
@@ -1501,7 +1544,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_kernel(const __
     else if (threadIdx.x < NTG + 32)
         mma_role<false>(S, P.status);
     else
-        tile_role<NTG * PP / 128, false>(F, S, P.status);
+        tile_role<NTG * PP / 128, false, CUSP>(F, S, P.status);
     cta_teardown(S, tm_cols);
 }
 
@@ -1536,7 +1579,7 @@ __global__ void __launch_bounds__(cta_threads(NTG), 1) rho_mixed_batch_kernel(co
     else if (threadIdx.x < NTG + 32)
         mma_role<true>(S, P.status);
     else
-        tile_role<NTG * PP / 128, true>(F, S, P.status);
+        tile_role<NTG * PP / 128, true, CUSP>(F, S, P.status);
     cta_teardown(S, 512);
 }
 
@@ -2016,7 +2059,8 @@ extern "C" int okg_batch_status(okg_batch* b, int* device_status)
     *device_status = v;
     if (v) {
         cudaMemset(b->d_status, 0, sizeof(int));
-        return set_error(OKG_ERR_TIMEOUT, "okg_batch_run: a tensor-core wait timed out");
+        if (v & 1) return set_error(OKG_ERR_TIMEOUT, "okg_batch_run: a tensor-core wait timed out");
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_batch_run: more than 8 cusp atoms in one 128-point tile");
     }
     return OKG_OK;
 }
@@ -2030,7 +2074,8 @@ extern "C" int okg_mixed_status(okg_mixed_plan* p, int* device_status)
     *device_status = v;
     if (v) {
         cudaMemset(p->status, 0, sizeof(int));
-        return set_error(OKG_ERR_TIMEOUT, "okg_rho_mixed: a tensor-core wait timed out");
+        if (v & 1) return set_error(OKG_ERR_TIMEOUT, "okg_rho_mixed: a tensor-core wait timed out");
+        return set_error(OKG_ERR_UNSUPPORTED, "okg_rho_mixed: more than 8 cusp atoms in one 128-point tile");
     }
     return OKG_OK;
 }
