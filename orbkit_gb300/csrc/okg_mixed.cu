@@ -901,7 +901,7 @@ __device__ __forceinline__ void steep_shells(const MolDesc& D, int a, double rr,
 // tile's cusp atoms, contracted with C_eff in FP64 for the MOs [mo0, mo0 + 8).  Used when
 // the point has more steep components than a CuspVals holds (not inlined: its
 // registers stay out of the epilogue's budget).
-__device__ __noinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo0, int ch, double* out)
+__device__ __forceinline__ void cusp_part(const MolDesc& D, const EpiPt& ep, int mo0, int ch, double* out)
 {
     const BasisDev& B = D.B;
 #pragma unroll
@@ -937,7 +937,7 @@ struct CuspVals {
     double v[MAX_SC][4];
 };
 
-__device__ __noinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, CuspVals& cz)
+__device__ __forceinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, CuspVals& cz)
 {
     const BasisDev& B = D.B;
     cz.n = 0;
@@ -963,7 +963,7 @@ __device__ __noinline__ void cusp_prepare(const MolDesc& D, const EpiPt& ep, Cus
 }
 
 // out[i] = sum over the prepared components of C_eff[mo0 + i][col] x value (channel ch).
-__device__ __noinline__ void cusp_contract(const MolDesc& D, const CuspVals& cz, int mo0, int ch, double* out)
+__device__ __forceinline__ void cusp_contract(const MolDesc& D, const CuspVals& cz, int mo0, int ch, double* out)
 {
 #pragma unroll
     for (int i = 0; i < 8; ++i) out[i] = 0.0;
