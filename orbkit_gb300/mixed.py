@@ -234,19 +234,22 @@ class MixedEvaluator:
     def _cusp_fix(self, g, rho, grad):
         import torch
         # cached per regular grid (its axes) or per vector-grid object (held here, so
-        # its identity is not reused), and per geometry and radius
+        # its identity is not reused), and per geometry and radius; a few grids are
+        # kept (the x slabs of a pipelined evaluation are grids of their own)
         key = (self.cusp_radius, self.geo.tobytes(),
                tuple(numpy.ascontiguousarray(v).tobytes() for v in g.host) if g.regular else id(g))
-        if getattr(self, "_cusp_key", None) != key:
-            self._cusp_grid = g
-            self._cusp_key = key
+        cache = self.__dict__.setdefault("_cusp_cache", {})
+        if key not in cache:
+            if len(cache) >= 16:
+                cache.pop(next(iter(cache)))
             idx, pts = cusp_points(self.geo, g, self.cusp_radius, self.device)
             m = len(idx)
             r = torch.empty(m, dtype=torch.float64, device=self.device)
             dr = torch.empty((3, m), dtype=torch.float64, device=self.device)
             gd = _lib.OkgGrid(pts[0].data_ptr(), pts[1].data_ptr(), pts[2].data_ptr(), m, 0, 0, 0, 0, 0)
-            self._cusp = (idx, pts, r, dr, gd, _lib.int_array([1, 2, 3]))
-        idx, pts, r, dr, gd, codes = self._cusp
+            cache[key] = (idx, pts, r, dr, gd, _lib.int_array([1, 2, 3]), None if g.regular else g)
+        idx, pts, r, dr, gd, codes, _ = cache[key]
+        self._cusp = cache[key]
         m = len(idx)
         if m == 0:
             return
@@ -256,13 +259,68 @@ class MixedEvaluator:
         rho.index_copy_(0, idx, r)
         grad.index_copy_(1, idx, dr)
 
-    def evaluate(self, x, y, z, is_vector, out=None):
-        """Host grid in, host (rho, grad) out.  `out` may hold preallocated (pinned)
-        host tensors (rho (npts,), grad (3, npts)) that receive the results."""
+    SLABS = 4  # x slabs of a pipelined regular-grid evaluation
+
+    def _evaluate_slabs(self, x, y, z, out):
+        """Regular grid in x slabs (each a regular grid of its own, brick-tiled), the
+        read-back of one slab on a second stream while the next slab's kernel runs."""
         import torch
         from .core import _DeviceGrid
-        g = _DeviceGrid(numpy.asarray(x, dtype=numpy.float64), numpy.asarray(y, dtype=numpy.float64),
-                        numpy.asarray(z, dtype=numpy.float64), is_vector, self.device)
+        nx, nyz = len(x), len(y) * len(z)
+        n = nx * nyz
+        cuts = sorted({min(nx, 4 * round(nx * i / (4 * self.SLABS))) for i in range(self.SLABS + 1)} | {0, nx})
+        bufs = getattr(self, "_slab_bufs", None)
+        if bufs is None or bufs[0].numel() != n:
+            bufs = (torch.empty(n, dtype=torch.float64, device=self.device),
+                    torch.empty((3, n), dtype=torch.float64, device=self.device))
+            self._slab_bufs = bufs
+        rho, grad = bufs
+        if getattr(self, "_copy_stream", None) is None:
+            self._copy_stream = torch.cuda.Stream(device=self.device)
+        comp, copy = torch.cuda.current_stream(), self._copy_stream
+        keep = []
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            if b <= a:
+                continue
+            g = _DeviceGrid(x[a:b], y, z, False, self.device)
+            s0, s1 = a * nyz, b * nyz
+            gd, kg = g.slice(0, s1 - s0)
+            keep.append((g, kg))
+            rv, gv = rho[s0:s1], grad[:, s0:s1]
+            self.plan.rho(gd, rv, gv, n)
+            if self.cusp_radius and self.cusp_radius > 0:
+                self._cusp_fix(g, rv, gv)
+            done = torch.cuda.Event()
+            done.record(comp)
+            copy.wait_event(done)
+            with torch.cuda.stream(copy):
+                out[0][s0:s1].copy_(rv, non_blocking=True)
+                for c in range(3):
+                    out[1][c, s0:s1].copy_(grad[c, s0:s1], non_blocking=True)
+        copy.synchronize()
+        # the next call's kernels must not overwrite the buffers before these copies end
+        comp.wait_stream(copy)
+        return out
+
+    def evaluate(self, x, y, z, is_vector, out=None):
+        """Host grid in, host (rho, grad) out.  `out` may hold preallocated (pinned)
+        host tensors (rho (npts,), grad (3, npts)) that receive the results.  A regular
+        grid with the FP64 recomputation of its cusp points is evaluated in x slabs whose
+        read-backs overlap the following slabs' kernels."""
+        import torch
+        from .core import _DeviceGrid
+        x = numpy.asarray(x, dtype=numpy.float64)
+        y = numpy.asarray(y, dtype=numpy.float64)
+        z = numpy.asarray(z, dtype=numpy.float64)
+        if not is_vector and self.cusp_mode == "recompute" and len(x) >= 8 * self.SLABS:
+            npts = len(x) * len(y) * len(z)
+            if out is None:
+                out = (torch.empty(npts, dtype=torch.float64, pin_memory=True),
+                       torch.empty((3, npts), dtype=torch.float64, pin_memory=True))
+                self._evaluate_slabs(x, y, z, out)
+                return out[0].numpy(), out[1].numpy()
+            return self._evaluate_slabs(x, y, z, out)
+        g = _DeviceGrid(x, y, z, is_vector, self.device)
         rho, grad = self.evaluate_device(g)
         if out is None:
             # page-locked host arrays from torch's caching host allocator (reused
