@@ -151,6 +151,28 @@ def cusp_points_regular(geo, x, y, z, radius):
     return numpy.unique(numpy.concatenate(out))
 
 
+class _Slab:
+    """x slab [a, b) of a regular grid already on the device: a regular grid of its own
+    whose x axis starts at element a of the device x axis (no upload)."""
+
+    def __init__(self, full, x, y, z, a, b):
+        self.full = full
+        self.regular = True
+        self.host = (x[a:b], y, z)
+        self.shape = (b - a, len(y), len(z))
+        self.npts = (b - a) * len(y) * len(z)
+        self.a = a
+
+    def grid(self):
+        xd, yd, zd = self.full.dev
+        g = _lib.OkgGrid()
+        g.d_x, g.d_y, g.d_z = xd.data_ptr() + 8 * self.a, yd.data_ptr(), zd.data_ptr()
+        g.npts, g.offset = self.npts, 0
+        g.nx, g.ny, g.nz = self.shape
+        g.regular = 1
+        return g
+
+
 class MixedEvaluator:
     """Device resources for repeated mixed-precision rho / grad rho evaluation of
     one molecule: the packed basis, the tensor-core coefficient plan and output
@@ -278,14 +300,13 @@ class MixedEvaluator:
         if getattr(self, "_copy_stream", None) is None:
             self._copy_stream = torch.cuda.Stream(device=self.device)
         comp, copy = torch.cuda.current_stream(), self._copy_stream
-        keep = []
+        full = _DeviceGrid(x, y, z, False, self.device)  # the three axes, uploaded once
         for a, b in zip(cuts[:-1], cuts[1:]):
             if b <= a:
                 continue
-            g = _DeviceGrid(x[a:b], y, z, False, self.device)
+            g = _Slab(full, x, y, z, a, b)
             s0, s1 = a * nyz, b * nyz
-            gd, kg = g.slice(0, s1 - s0)
-            keep.append((g, kg))
+            gd = g.grid()
             rv, gv = rho[s0:s1], grad[:, s0:s1]
             self.plan.rho(gd, rv, gv, n)
             if self.cusp_radius and self.cusp_radius > 0:
