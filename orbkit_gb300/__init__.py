@@ -58,8 +58,10 @@ def install(orbkit_module):
     saved_grid = ours_core.grid
     ours_core.grid = orbkit_module.grid
     saved_display = ours_core.display
+    saved_options = ours_core._orbkit_options
     try:
         ours_core.display = importlib.import_module(orbkit_module.__name__ + ".display").display
+        ours_core._orbkit_options = importlib.import_module(orbkit_module.__name__ + ".options")
     except (ImportError, AttributeError):
         pass
 
@@ -68,5 +70,6 @@ def install(orbkit_module):
             setattr(obj, n, f)
         ours_core.grid = saved_grid
         ours_core.display = saved_display
+        ours_core._orbkit_options = saved_options
 
     return restore

@@ -34,6 +34,8 @@ MAX_SLICE_BYTES = 4 << 30
 # orbkit's terminal output (orbkit/display.py: display); install() routes it to
 # orbkit's own display, which honours orbkit.options.quiet and the .oklog file
 quiet = False
+# orbkit's options module once install(orbkit) routed display to orbkit's own
+_orbkit_options = None
 
 
 def display(msg):
@@ -41,10 +43,18 @@ def display(msg):
         print(msg)
 
 
+def _displaying():
+    """Whether a message would be shown or logged (the norms and the electron count are
+    only summed when it would)."""
+    if _orbkit_options is not None:
+        return not (getattr(_orbkit_options, "quiet", False) and getattr(_orbkit_options, "no_log", False))
+    return not quiet
+
+
 def _report(rho, mo_norm, mo_spec, d3r, was_vector, drv, calc_ao=False):
     """The MO norms (regular grid, no derivatives) and the electron count (regular
     grid) that orbkit's rho_compute prints (orbkit/core.py:572-592)."""
-    if was_vector:
+    if was_vector or not _displaying():
         return
     if drv is None and mo_norm is not None:
         display("\nNorm of the MOs:")
@@ -394,14 +404,14 @@ def rho_compute_no_slice(qc, calc_ao=False, calc_mo=False, drv=None, laplacian=F
     for v in (x, y, z):
         if len(v) > 1:
             d3r *= v[1] - v[0]
-    if mo_list is not None and not vec:
+    if mo_list is not None and not vec and _displaying():
         _report_norms_no_slice(numpy.array([numpy.sum(m ** 2) for m in mo_list]), mo_spec, d3r)
     if calc_mo:
         return (ao_list, mo_list) if return_components else mo_list
     rcodes = [] if drv is None else codes
     res = _eval(geo, ao_spec, mo_spec, x, y, z, vec, "rho", rcodes, exact_mixed, mo_norm=mo_list is None and not vec)
     rho, drho = res[0], res[1]
-    if not vec:
+    if not vec and _displaying():
         if mo_list is None:
             _report_norms_no_slice(res[2], mo_spec, d3r)
         display("We have " + str(numpy.sum(rho) * d3r) + " electrons.")
