@@ -281,7 +281,7 @@ class MixedEvaluator:
         rho.index_copy_(0, idx, r)
         grad.index_copy_(1, idx, dr)
 
-    SLABS = 4  # x slabs of a pipelined regular-grid evaluation
+    SLABS = 2  # x slabs of a pipelined regular-grid evaluation
 
     def _evaluate_slabs(self, x, y, z, out):
         """Regular grid in x slabs (each a regular grid of its own, brick-tiled), the
