@@ -32,12 +32,13 @@
 // buffers of tile index, descriptor and screening tables, handed over through
 // "screened" and "kfree" mbarriers).  Generation threads and the MMA warp are
 // connected by a two-stage ring in shared memory:
-//   * generation threads write 4 channels x 3 parts of A (128 x 32 BF16, K-major,
-//     SWIZZLE_64B) for a chunk into a free stage and arrive on its "full" barrier;
+//   * generation threads write 4 channels x 3 parts of A (128 x 32 BF16, M-major,
+//     SWIZZLE_128B) for a chunk into a free stage and arrive on its "full" barrier;
 //   * the MMA warp bulk-copies the chunk's pre-split, pre-swizzled B block into the
-//     stage (columns of screened shells then zeroed), waits for "full", issues 48 MMAs
-//     from one thread and commits them to the stage's "empty" barrier, so the
-//     tensor core works on one chunk while the next one is generated;
+//     stage (columns of screened shells then zeroed), waits for "full", issues up to
+//     48 MMAs from one thread (descriptors advanced in their 32-bit address word) and
+//     commits them to the stage's "empty" barrier, so the tensor core works on one
+//     chunk while the next one is generated;
 //   * after the last chunk of an MO pass the MMA warp commits to "acc full"; the
 //     generation warps read the accumulators (8 x N FP32 columns of TMEM: value
 //     4 leading + 1 correction; d/dx, d/dy, d/dz), arrive on "acc empty" and
@@ -113,6 +114,18 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
         "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// The same MMA with the descriptors as (address word, upper word) pairs: offsets
+// inside a stage are added to the address word alone (the start address field,
+// shared address >> 4, stays below 2^14 and never carries into the upper bits).
+__device__ __forceinline__ void mma_bf16_w(uint32_t d_tmem, uint32_t a_lo, uint32_t a_hi, uint32_t b_lo, uint32_t b_hi,
+                                           uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t.reg .b64 ad, bd;\n\tmov.b64 ad, {%1, %2};\n\tmov.b64 bd, {%3, %4};\n\t"
+        "setp.ne.b32 p, %6, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n\t}\n" ::"r"(d_tmem),
+        "r"(a_lo), "r"(a_hi), "r"(b_lo), "r"(b_hi), "r"(idesc), "r"(acc));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar)
@@ -772,9 +785,9 @@ __device__ __forceinline__ void shell_eval2_L(int L, const float (&X)[2], const 
 }
 
 // Generation threads: the AO values (4 or 1 channels x 3 BF16 parts) of one kept
-// chunk for this thread's P points and atoms, into the next stage of the ring.
-// With P = 2 the two points are adjacent in the M-major tile: each part of a
-// value pair is one packed conversion and one 4-byte store.
+// chunk for this thread's P points and atoms, into the next
+// stage of the ring.  With P = 2 the two points are adjacent in the M-major tile:
+// each part of a value pair is one packed conversion and one 4-byte store.
 template <int NTG, int P>
 __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char* nkeep, int c, const CtaState& S,
                                           uint32_t& seq, AtomRun<P>& ar, unsigned chmask, const GenPts<P>& gp,
@@ -1086,100 +1099,102 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
     mbar_arrive(S.bar_acc_empty);
 }
 
+// A job of the generation side: one MO pass of one tile.
+struct GenJob {
+    uint32_t ord;   // tile ordinal of the CTA
+    int pass;
+    int nch, nks;   // chunks and K-steps generated so far
+    long long p;    // this thread's output point (epilogue row)
+    bool valid;
+};
+
 // Generation side of the CTA.  Jobs (tile, MO pass) are generated in order; the
 // first chunk of the next job (screening its tile first when it starts one) is
-// generated before the epilogue of the current job, so the tensor core's tail
-// of a job overlaps useful work.
+// generated before the epilogue of the current job, so the tensor core's tail of a
+// job overlaps useful work.  The loop has one call site each for chunk generation
+// and the epilogue (both are large inlined bodies: a second copy of either doubles
+// the hot instruction footprint of the generation warps).
 template <int NTG, int P, bool BATCH, bool CUSP>
 __device__ __forceinline__ void gen_role(const CtaState& S, int* status)
 {
     constexpr int E = NTG / 128;  // epilogue warps per TMEM lane quarter
     const int warp = threadIdx.x >> 5;
     const int h = warp >> 2;
-    uint32_t seq = 0, accseq = 0, ord = 0;
-    long long p = 0;
-    bool valid = false;
+    uint32_t seq = 0, accseq = 0;
     GenPts<P> gp;
-    EpiPt ep, ep_next;
-    CuspVals cz;  // the current tile's steep AO values at this thread's cusp point
-    cz.n = -2;    // -2: not prepared for the current tile yet
-    if (gen_open_tile<P, BATCH, CUSP>(S, ord, p, valid, gp, ep, status) < 0) return;
-    int gpass = 0;
+    EpiPt ep, ep_g;  // points of the epilogue's tile and of the generated job's tile
+    CuspVals cz;     // the epilogue tile's steep AO values at this thread's cusp point
+    cz.n = -2;       // -2: not prepared for the current tile yet
+    GenJob g{0u, 0, 0, 0, 0, false}, e = g;  // the job being generated, the job whose epilogue is due
+    if (gen_open_tile<P, BATCH, CUSP>(S, 0u, g.p, g.valid, gp, ep, status) < 0) return;
     AtomRun<P> ar;
     int c = next_kept(S.kmask, S.mol[0].B.nmchunk, -1);
-    int nch = 0, nks = 0;  // chunks and K-steps issued in the current job
+    bool due = false, more = true;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     for (;;) {
-        const MolDesc& Dg = S.mol[BATCH ? tbuf(ord) : 0];
-        const unsigned* km = S.kmask + tbuf(ord) * MAX_CHUNKS;
-        {
-            const unsigned chmask = Dg.want_grad ? 0xFu : 0x1u;
-            const BasisDev& B = Dg.B;
-            const unsigned char* nkeep = S.nkeep + tbuf(ord) * MAX_SHELLS;
-            while (c >= 0 && !warp_aborted(S.abort_flag)) {
-                gen_chunk<NTG, P>(B, nkeep, c, S, seq, ar, chmask, gp, status);
-                ++nch;
-                nks += ksteps_of(km[c]);
-                c = next_kept(km, B.nmchunk, c);
+        if (c >= 0) {
+            const MolDesc& Dg = S.mol[BATCH ? tbuf(g.ord) : 0];
+            const unsigned* km = S.kmask + tbuf(g.ord) * MAX_CHUNKS;
+            if (warp_aborted(S.abort_flag)) {
+                c = -1;
+            } else {
+                gen_chunk<NTG, P>(Dg.B, S.nkeep + tbuf(g.ord) * MAX_SHELLS, c, S, seq, ar,
+                                  Dg.want_grad ? 0xFu : 0x1u, gp, status);
+                ++g.nch;
+                g.nks += ksteps_of(km[c]);
+                c = next_kept(km, Dg.B.nmchunk, c);
+            }
+        } else if (!due) {
+            // every chunk of job g is out
+            const MolDesc& Dg = S.mol[BATCH ? tbuf(g.ord) : 0];
+            // single molecule: the tile's screening tables are not read after its last
+            // chunk, so the buffer is released now and the tile warp screens ahead during
+            // this job's epilogue (a batch releases after the stores: the buffer also holds
+            // the molecule's descriptor)
+            if (!BATCH && g.pass == Dg.npass - 1) mbar_arrive(S.bar_kfree + 8 * tbuf(g.ord));
+            // the next job: the next MO pass of this tile, or pass 0 of a new tile
+            GenJob n = g;
+            n.pass = g.pass + 1;
+            n.nch = n.nks = 0;
+            if (n.pass == Dg.npass) {
+                n.ord = g.ord + 1;
+                n.pass = 0;
+                more = gen_open_tile<P, BATCH, CUSP>(S, n.ord, n.p, n.valid, gp, ep_g, status) >= 0;
+            }
+            e = g;
+            due = true;
+            if (more) {
+                g = n;
+                ar = AtomRun<P>();
+                c = next_kept(S.kmask + tbuf(g.ord) * MAX_CHUNKS, S.mol[BATCH ? tbuf(g.ord) : 0].B.nmchunk, -1);
             }
         }
-        // single molecule: the tile's screening tables are not read after its last
-        // chunk, so the buffer is released now and the tile warp screens ahead
-        // during this job's epilogue (a batch releases after the stores: the buffer
-        // also holds the molecule's descriptor)
-        if (!BATCH && gpass == Dg.npass - 1) mbar_arrive(S.bar_kfree + 8 * tbuf(ord));
-        // the next job: the next MO pass of this tile, or pass 0 of a new tile
-        int npass_next = gpass + 1;
-        uint32_t ord_next = ord;
-        long long p_next = p;
-        bool valid_next = valid, more = true;
-        if (npass_next == Dg.npass) {
-            ord_next = ord + 1;
-            npass_next = 0;
-            more = gen_open_tile<P, BATCH, CUSP>(S, ord_next, p_next, valid_next, gp, ep_next, status) >= 0;
-        }
-        int c_next = -1, nch_next = 0, nks_next = 0;
-        if (more) {
-            const MolDesc& Dn = S.mol[BATCH ? tbuf(ord_next) : 0];
-            const unsigned* kmn = S.kmask + tbuf(ord_next) * MAX_CHUNKS;
-            ar = AtomRun<P>();
-            c_next = next_kept(kmn, Dn.B.nmchunk, -1);
-            if (c_next >= 0) {
-                gen_chunk<NTG, P>(Dn.B, S.nkeep + tbuf(ord_next) * MAX_SHELLS, c_next, S, seq, ar,
-                                  Dn.want_grad ? 0xFu : 0x1u, gp, status);
-                ++nch_next;
-                nks_next += ksteps_of(kmn[c_next]);
-                c_next = next_kept(kmn, Dn.B.nmchunk, c_next);
-            }
-        }
-        // the current job's epilogue (nothing to read if none of its chunks reached the tile)
-        if (nch > 0) gen_epilogue<E, CUSP>(Dg, gpass, nks, S, accseq, acc, ep, cz, status);
-        if (gpass == Dg.npass - 1) {
-            if (valid && !*S.abort_flag) {
-                if (0 % E == h) Dg.rho[p] = acc[0];
-                if (Dg.want_grad) {
+        // job e's epilogue once the next job's first chunk is out (or it has none)
+        if (due && (g.nch > 0 || c < 0 || !more)) {
+            const MolDesc& De = S.mol[BATCH ? tbuf(e.ord) : 0];
+            // (nothing to read if none of its chunks reached the tensor core)
+            if (e.nch > 0) gen_epilogue<E, CUSP>(De, e.pass, e.nks, S, accseq, acc, ep, cz, status);
+            if (e.pass == De.npass - 1) {
+                if (e.valid && !*S.abort_flag) {
+                    if (0 % E == h) De.rho[e.p] = acc[0];
+                    if (De.want_grad) {
 #pragma unroll
-                    for (int o = 1; o < 4; ++o)
-                        if (o % E == h) Dg.grad[(long long)(o - 1) * Dg.ld + p] = acc[o];
+                        for (int o = 1; o < 4; ++o)
+                            if (o % E == h) De.grad[(long long)(o - 1) * De.ld + e.p] = acc[o];
+                    }
                 }
-            }
 #pragma unroll
-            for (int o = 0; o < 4; ++o) acc[o] = 0.0;
-            // this thread is done with the tile's buffer (descriptor, screening tables)
-            if (BATCH) mbar_arrive(S.bar_kfree + 8 * tbuf(ord));
+                for (int o = 0; o < 4; ++o) acc[o] = 0.0;
+                // this thread is done with the tile's buffer (descriptor, screening tables)
+                if (BATCH) mbar_arrive(S.bar_kfree + 8 * tbuf(e.ord));
+            }
+            due = false;
+            if (!more) break;
+            if (g.ord != e.ord) {
+                ep = ep_g;
+                cz.n = -2;
+            }
         }
-        if (!more) break;
-        gpass = npass_next;
-        if (ord_next != ord) {
-            ep = ep_next;
-            cz.n = -2;
-        }
-        ord = ord_next;
-        p = p_next;
-        valid = valid_next;
-        c = c_next;
-        nch = nch_next;
-        nks = nks_next;
     }
 }
 
@@ -1255,10 +1270,51 @@ __device__ __forceinline__ bool mma_prefetch_b(const CtaState& S, const MmaItem&
     return true;
 }
 
+// One chunk's MMAs from one thread: per issued K-step and channel the six
+// (A part, B part) products b0c0 b0c1 b1c0 b0c2 b1c1 b2c0.  The value channel's
+// leading product goes to accumulator ks mod 4 (ks: K-step of the job), its five
+// corrections to accumulator 4; gradient channel ch takes all six in accumulator
+// 4 + ch.  after_first() runs once, after the first issued K-step.  The loops stay
+// rolled: the warp shares its SM sub-partition's instruction cache with generation
+// warps.
+template <typename F>
+__device__ __forceinline__ void mma_issue_chunk(uint32_t tmem, int npad, int nch, uint32_t a_lo, uint32_t a_hi,
+                                                uint32_t b_lo, uint32_t b_hi, unsigned km, int kq, F&& after_first)
+{
+    const uint32_t idesc = idesc_bf16(M, npad);
+    const uint32_t bpart = (uint32_t)(npad * ROWB) >> 4;
+    constexpr uint32_t apart = A_TILE >> 4;
+    const bool kon0 = (km & 0xFFFFu) != 0u, kon1 = (km >> 16) != 0u;
+    bool first = true;
+#pragma unroll 1
+    for (int k = 0; k < KC / 16; ++k) {
+        if (!(k == 0 ? kon0 : kon1)) continue;  // all 16 columns screened
+        const int ks = kq + (k == 1 && kon0);
+        const uint32_t f0 = ks > 0;
+        const uint32_t bk = b_lo + (uint32_t)((k * 32) >> 4);
+#pragma unroll 1
+        for (int ch = 0; ch < nch; ++ch) {
+            const uint32_t a0 = a_lo + (uint32_t)((ch * 3 * A_TILE + k * 4096) >> 4);
+            const uint32_t dc = tmem + (uint32_t)((4 + ch) * npad);  // corrections / gradient
+            const uint32_t dl = ch == 0 ? tmem + (uint32_t)((ks & 3) * npad) : dc;
+            const uint32_t fl = ch == 0 ? (uint32_t)(ks >= 4) : f0;
+            const uint32_t f1 = ch == 0 ? f0 : 1u;
+            mma_bf16_w(dl, a0, a_hi, bk, b_hi, idesc, fl);
+            mma_bf16_w(dc, a0, a_hi, bk + bpart, b_hi, idesc, f1);
+            mma_bf16_w(dc, a0 + apart, a_hi, bk, b_hi, idesc, 1u);
+            mma_bf16_w(dc, a0, a_hi, bk + 2 * bpart, b_hi, idesc, 1u);
+            mma_bf16_w(dc, a0 + apart, a_hi, bk + bpart, b_hi, idesc, 1u);
+            mma_bf16_w(dc, a0 + 2 * apart, a_hi, bk, b_hi, idesc, 1u);
+        }
+        if (first) after_first();
+        first = false;
+    }
+}
+
 // MMA side of the CTA (the last warp): for every kept chunk in order, the column
-// mask applied to its B block, then 48 MMAs (12 without gradient) from lane 0
-// once the generation threads filled the stage; the next chunk's B block is
-// requested halfway through, when the stage it goes to has been consumed.
+// mask applied to its B block, then 48 MMAs (12 without gradient) from lane 0 once
+// the generation threads filled the stage; the next chunk's B block is requested
+// halfway through, when the stage it goes to has been consumed.
 template <bool BATCH>
 __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
 {
@@ -1278,13 +1334,13 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
         const uint32_t s = seq & 1u, u = seq >> 1;
         unsigned char* B_s = S.B_s + s * B_STAGE;
         const int npad = cur.npad;
-        const int bunits = 3 * npad * RUNITS;
         const bool landed = mbar_wait(S.bar_bload + 8 * s, u & 1u, status, S.wait_limit);
         if (!__all_sync(0xffffffffu, landed)) {
             *S.abort_flag = 1;
             break;
         }
         if (pend == (long long)seq) pend = -1;
+        const int bunits = 3 * npad * RUNITS;
         // columns of screened shells are zeroed.  Lane l touches the 16-byte units
         // l, l + 32, ...: rows n = l / 4 (mod 8) of every part, physical unit l % 4, so
         // with rows of 4 units and the 64-byte swizzle (unit ^ (n >> 1) % 4) always the
@@ -1316,43 +1372,14 @@ __device__ __forceinline__ void mma_role(const CtaState& S, int* status)
                 *S.abort_flag = 1;
             if (!mbar_wait(S.bar_full + 8 * s, u & 1u, status, S.wait_limit)) *S.abort_flag = 1;
             tc_fence_after();
-            const int nch = cur.nch;
-            const int pf = nch > 2 ? 1 : nch - 1;  // channel after which the next B block is requested
-            const bool kon[2] = {(cur.km & 0xFFFFu) != 0u, (cur.km >> 16) != 0u};
             if (!*S.abort_flag) {
-                const uint32_t idesc = idesc_bf16(M, npad);
-                const uint32_t bpart16 = (uint32_t)(npad * ROWB) >> 4;
-                // descriptors differ only in the start-address field (bytes >> 4)
-                const uint64_t adesc = adesc_mn(smem_u32(S.A_s + s * A_STAGE)), bdesc = sdesc(smem_u32(B_s));
-#pragma unroll 1
-                for (int ch = 0; ch < nch; ++ch) {
-#pragma unroll
-                    for (int k = 0; k < KC / 16; ++k) {
-                        if (!kon[k]) continue;  // all 16 columns screened
-                        const int ks = kq + (k == 1 && kon[0]);
-                        // (a part, b part) pairs: b0c0 b0c1 b1c0 b0c2 b1c1 b2c0
-                        const int pa[6] = {0, 0, 1, 0, 1, 2};
-                        const int pb[6] = {0, 1, 0, 2, 1, 0};
-#pragma unroll
-                        for (int t = 0; t < 6; ++t) {
-                            const uint64_t ad = adesc + (uint64_t)(((ch * 3 + pa[t]) * A_TILE + k * 4096) >> 4);
-                            const uint64_t bd = bdesc + (uint64_t)(pb[t] * bpart16 + ((k * 32) >> 4));
-                            uint32_t col, accf;
-                            if (ch == 0 && t == 0) {  // leading product -> accumulator ks mod 4
-                                col = ks & 3;
-                                accf = ks >= 4;
-                            } else if (ch == 0) {     // value corrections -> accumulator 4
-                                col = 4;
-                                accf = ks > 0 || t > 1;
-                            } else {                  // gradient channel ch -> accumulator 4 + ch
-                                col = 4 + ch;
-                                accf = ks > 0 || t > 0;
-                            }
-                            mma_bf16(S.tmem + col * npad, ad, bd, idesc, accf);
-                        }
-                    }
-                    if (ch == pf && in_tile && mma_prefetch_b(S, nxt, seq + 1, status)) pend = seq + 1;
-                }
+                const uint64_t ad = adesc_mn(smem_u32(S.A_s + s * A_STAGE)), bd = sdesc(smem_u32(B_s));
+                // the next chunk's B block is requested once the first K-step is out
+                auto prefetch = [&]() {
+                    if (in_tile && mma_prefetch_b(S, nxt, seq + 1, status)) pend = seq + 1;
+                };
+                mma_issue_chunk(S.tmem, npad, cur.nch, (uint32_t)ad, (uint32_t)(ad >> 32), (uint32_t)bd,
+                                (uint32_t)(bd >> 32), cur.km, kq, prefetch);
                 issued = true;
                 mma_commit(S.bar_empty + 8 * s);
             } else {
