@@ -90,6 +90,15 @@ int okg_basis_info(const okg_basis* basis, int* ncart, int* nao, int* nshell, in
  * ordered after this one (same stream, or synchronised). */
 int okg_basis_set_params(okg_basis* basis, const double* d_geo, const double* d_prim, okg_stream stream);
 
+/* Column order of the mixed (tensor-core) path: h_order (nshell, host) is a
+ * permutation of the shells; whole shells are packed in that order into chunks of
+ * 32 columns.  The order changes which K-steps a grid tile's kept shells occupy
+ * (the tensor-core work), not the results beyond FP32 summation order.  Only
+ * before a mixed plan (okg_mixed_plan_create*, okg_batch_*) or okg_rho_mixed_noalloc
+ * used the basis: OKG_ERR_ARG after that, or if h_order is not a permutation.
+ * Synchronous (host-to-device copies).  No orbkit counterpart (layout hint). */
+int okg_basis_set_mixed_order(okg_basis* basis, const int* h_order);
+
 /* AOs and AO derivatives on a grid, FP64.
  * Replaces cy_core.aocreator + c_lcreator (orbkit/cy_core.pyx:51-78,
  * orbkit/c_grid-based.c:9-79) followed by the 'N' factor and cartesian2spherical

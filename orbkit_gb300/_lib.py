@@ -42,6 +42,7 @@ SIGNATURES = {
     "okg_basis_destroy": (ctypes.c_int, [_vp]),
     "okg_basis_info": (ctypes.c_int, [_vp, _c_int_p, _c_int_p, _c_int_p, _c_int_p, _c_int_p]),
     "okg_basis_set_params": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "okg_basis_set_mixed_order": (ctypes.c_int, [_vp, _vp]),
     "okg_eval_ao": (ctypes.c_int, [_vp, ctypes.POINTER(OkgGrid), ctypes.c_int, _c_int_p, ctypes.c_int, _vp,
                                    ctypes.c_int64, _vp]),
     "okg_eval_mo": (ctypes.c_int, [_vp, ctypes.POINTER(OkgGrid), ctypes.c_int, _vp, ctypes.c_int, _c_int_p,

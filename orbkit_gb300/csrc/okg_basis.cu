@@ -147,6 +147,70 @@ struct Layout {
         return o;
     }
 };
+
+// Mixed-path column layout for a shell order: whole shells, in that order, packed
+// into chunks of at most OKG_MKC canonical columns; per chunk column, the listed
+// Cartesian row it feeds (or -1) and its angular norm.  At most one chunk per shell.
+struct MixedLayout {
+    std::vector<Shell> mshells;
+    std::vector<int4> mchunks;
+    std::vector<int> mcol_cart;
+    std::vector<double> mcol_g;
+};
+
+MixedLayout mixed_layout(const std::vector<Shell>& shells, const std::vector<int>& comp_row,
+                         const std::vector<double>& comp_g, const int* order)
+{
+    MixedLayout m;
+    const int n = (int)shells.size();
+    int s0 = 0, col = 0;
+    for (int i = 0; i <= n; ++i) {
+        const int nk = i < n ? ncanon(shells[order ? order[i] : i].L) : 0;
+        if (i == n || col + nk > OKG_MKC) {
+            m.mchunks.push_back(make_int4(s0, i, col, 0));
+            const size_t base = m.mcol_cart.size();
+            m.mcol_cart.resize(base + OKG_MKC, -1);
+            m.mcol_g.resize(base + OKG_MKC, 0.0);
+            for (int t = s0; t < i; ++t) {
+                const Shell& sh = m.mshells[t];
+                for (int q = 0; q < ncanon(sh.L); ++q) {
+                    const int r = comp_row[sh.comp0 + q];
+                    if (r >= 0) {
+                        m.mcol_cart[base + sh.mcol + q] = sh.cart0 + r;
+                        m.mcol_g[base + sh.mcol + q] = comp_g[sh.comp0 + q];
+                    }
+                }
+            }
+            s0 = i;
+            col = 0;
+        }
+        if (i < n) {
+            Shell sh = shells[order ? order[i] : i];
+            sh.mcol = col;
+            sh.mchunk = (int)m.mchunks.size();
+            m.mshells.push_back(sh);
+            col += nk;
+        }
+    }
+    return m;
+}
+
+// Upload a mixed layout into the basis block (capacity: one chunk per shell).
+cudaError_t upload_mixed(okg_basis* b, const MixedLayout& m)
+{
+    BasisDev& d = b->dev;
+    cudaError_t e = cudaMemcpy((void*)d.mshells, m.mshells.data(), sizeof(Shell) * m.mshells.size(),
+                               cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy((void*)d.mchunks, m.mchunks.data(), sizeof(int4) * m.mchunks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy((void*)d.mcol_cart, m.mcol_cart.data(), sizeof(int) * m.mcol_cart.size(),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy((void*)d.mcol_g, m.mcol_g.data(), sizeof(double) * m.mcol_g.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) d.nmchunk = (int)m.mchunks.size();
+    return e;
+}
 }  // namespace
 
 extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, const int* h_shell_ncart,
@@ -273,37 +337,8 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
         chunks.push_back(make_int4(s0, nshell, k0, k));
     }
 
-    // mixed-path chunks: whole shells, canonical columns, at most OKG_MKC per chunk
-    std::vector<int4> mchunks;
-    std::vector<int> mcol_cart;
-    std::vector<double> mcol_g;  // angular norm of each column (folded into the MO coefficients)
-    {
-        int s0 = 0, col = 0;
-        for (int s = 0; s <= nshell; ++s) {
-            const int nk = s < nshell ? ncanon(shells[s].L) : 0;
-            if (s == nshell || col + nk > OKG_MKC) {
-                mchunks.push_back(make_int4(s0, s, col, 0));
-                const size_t base = mcol_cart.size();
-                mcol_cart.resize(base + OKG_MKC, -1);
-                mcol_g.resize(base + OKG_MKC, 0.0);
-                for (int t = s0; t < s; ++t)
-                    for (int q = 0; q < ncanon(shells[t].L); ++q) {
-                        const int r = comp_row[shells[t].comp0 + q];
-                        if (r >= 0) {
-                            mcol_cart[base + shells[t].mcol + q] = shells[t].cart0 + r;
-                            mcol_g[base + shells[t].mcol + q] = comp_g[shells[t].comp0 + q];
-                        }
-                    }
-                s0 = s;
-                col = 0;
-            }
-            if (s < nshell) {
-                shells[s].mcol = col;
-                shells[s].mchunk = (int)mchunks.size();
-                col += nk;
-            }
-        }
-    }
+    // mixed-path chunks in basis order (okg_basis_set_mixed_order may choose another)
+    const MixedLayout mixed = mixed_layout(shells, comp_row, comp_g, nullptr);
 
     okg_basis* b = (okg_basis*)calloc(1, sizeof(okg_basis));
     if (!b) return set_error(OKG_ERR_ALLOC, "okg_basis_create: host allocation");
@@ -325,9 +360,10 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     const size_t o_asp = lay.take(sizeof(int) * (natom + 1));
     const size_t o_ash = lay.take(sizeof(int) * nshell);
     const size_t o_padj = lay.take(sizeof(double) * 2 * nprim);
-    const size_t o_mch = lay.take(sizeof(int4) * mchunks.size());
-    const size_t o_mcc = lay.take(sizeof(int) * mcol_cart.size());
-    const size_t o_mcg = lay.take(sizeof(double) * mcol_g.size());
+    const size_t o_msh = lay.take(sizeof(Shell) * nshell);
+    const size_t o_mch = lay.take(sizeof(int4) * nshell);
+    const size_t o_mcc = lay.take(sizeof(int) * OKG_MKC * nshell);
+    const size_t o_mcg = lay.take(sizeof(double) * OKG_MKC * nshell);
     const size_t bytes = lay.take(0);
     char* blk = nullptr;
     cudaError_t e = cudaMalloc((void**)&blk, bytes);
@@ -363,12 +399,12 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
         e = cudaMemcpy(blk + o_scoef, sph_coef.data(), sizeof(double) * sph_coef.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(blk + o_chunks, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(blk + o_mch, mchunks.data(), sizeof(int4) * mchunks.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(blk + o_mcc, mcol_cart.data(), sizeof(int) * mcol_cart.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(blk + o_mcg, mcol_g.data(), sizeof(double) * mcol_g.size(), cudaMemcpyHostToDevice);
+    BasisDev& d = b->dev;
+    d.mshells = (const Shell*)(blk + o_msh);
+    d.mchunks = (const int4*)(blk + o_mch);
+    d.mcol_cart = (const int*)(blk + o_mcc);
+    d.mcol_g = (const double*)(blk + o_mcg);
+    if (e == cudaSuccess) e = upload_mixed(b, mixed);
     if (e != cudaSuccess) {
         cudaFree(blk);
         free(b);
@@ -376,7 +412,6 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     }
     b->dev_block = blk;
     b->dev_bytes = bytes;
-    BasisDev& d = b->dev;
     d.atoms = (const double*)(blk + o_atoms);
     d.shells = (const Shell*)(blk + o_shells);
     d.prim = (const double*)(blk + o_prim);
@@ -393,10 +428,6 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     d.atom_shell_ptr = (const int*)(blk + o_asp);
     d.atom_shells = (const int*)(blk + o_ash);
     d.prim_adj = (const double*)(blk + o_padj);
-    d.mchunks = (const int4*)(blk + o_mch);
-    d.mcol_cart = (const int*)(blk + o_mcc);
-    d.mcol_g = (const double*)(blk + o_mcg);
-    d.nmchunk = (int)mchunks.size();
     d.natom = natom;
     d.nshell = nshell;
     d.nprim = nprim;
@@ -415,9 +446,35 @@ extern "C" int okg_basis_create(int natom, int nshell, const int* h_shell_atom, 
     for (int l = 0; l <= OKG_MAX_L; ++l) b->l_hist[l] = l_hist[l];
     b->is_normalized = is_normalized ? 1 : 0;
     b->prim_L = (int*)(blk + o_primL);
+    b->ncomp = (int)comp_row.size();
+    b->mixed_locked = 0;
     cudaGetDevice(&b->device);
     *out = b;
     return OKG_OK;
+}
+
+extern "C" int okg_basis_set_mixed_order(okg_basis* b, const int* h_order)
+{
+    if (!b || !h_order) return set_error(OKG_ERR_ARG, "okg_basis_set_mixed_order: NULL argument");
+    if (b->mixed_locked)
+        return set_error(OKG_ERR_ARG, "okg_basis_set_mixed_order: a mixed plan or evaluation already uses the basis");
+    const int n = b->nshell;
+    std::vector<char> seen(n, 0);
+    for (int i = 0; i < n; ++i) {
+        if (h_order[i] < 0 || h_order[i] >= n || seen[h_order[i]])
+            return set_error(OKG_ERR_ARG, "okg_basis_set_mixed_order: order is not a permutation of the shells");
+        seen[h_order[i]] = 1;
+    }
+    std::vector<Shell> shells(n);
+    std::vector<int> comp_row(b->ncomp);
+    std::vector<double> comp_g(b->ncomp);
+    cudaError_t e = cudaMemcpy(shells.data(), b->dev.shells, sizeof(Shell) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(comp_row.data(), b->dev.comp_row, sizeof(int) * b->ncomp, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(comp_g.data(), b->dev.comp_g, sizeof(double) * b->ncomp, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = upload_mixed(b, mixed_layout(shells, comp_row, comp_g, h_order));
+    return cuda_status(e, "okg_basis_set_mixed_order");
 }
 
 extern "C" int okg_basis_destroy(okg_basis* b)

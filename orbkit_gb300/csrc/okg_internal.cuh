@@ -50,8 +50,8 @@ struct Shell {
     int out0;   // first output row (Cartesian: cart0, spherical: first spherical row)
     int nout;   // output rows (ncart or number of spherical functions)
     int sph0;   // first spherical row's index into sph_ptr (spherical bases)
-    int mcol;   // mixed path: first column of this shell inside its chunk (canonical order)
-    int mchunk; // mixed path: index of the chunk holding this shell
+    int mcol;   // mixed path (records of BasisDev::mshells): first column of this shell inside its chunk
+    int mchunk; // mixed path (records of BasisDev::mshells): index of the chunk holding this shell
 };
 
 // Per-primitive data of the mixed path: alpha*log2(e) in FP64 (the exponent
@@ -79,7 +79,8 @@ struct BasisDev {
     const double2* prim_cusp;  // nprim (mixed path): {alpha, w} in FP64, in the order of prim_mx (ascending alpha per shell)
     const int* atom_shell_ptr; // natom + 1: shells of atom a are atom_shells[atom_shell_ptr[a] .. atom_shell_ptr[a+1])
     const int* atom_shells;    // nshell
-    const int4* mchunks;     // nmchunk x {first shell, end shell, used columns, 0} (mixed path, <= OKG_MKC columns)
+    const Shell* mshells;    // nshell: the shells in the mixed path's column order (okg_basis_set_mixed_order)
+    const int4* mchunks;     // nmchunk x {first, end index into mshells, used columns, 0} (<= OKG_MKC columns)
     const int* mcol_cart;    // nmchunk x OKG_MKC: listed Cartesian row feeding each column, or -1
     const double* mcol_g;    // nmchunk x OKG_MKC: angular norm of each column (0 where unused)
     int natom, nshell, nprim, ncart, nsph, spherical;
@@ -256,6 +257,8 @@ struct okg_basis {
     int natom, nshell, nprim, ncart, nao_out, max_l;
     int l_hist[OKG_MAX_L + 1];
     int device;
+    int ncomp;                 // entries of comp_row / comp_g
+    mutable int mixed_locked;  // a mixed plan or evaluation used the basis: its column order is fixed
 };
 
 namespace okg {

@@ -621,7 +621,7 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
         __syncwarp();
         // a primitive is kept while alpha log2(e) d^2 <= SCREEN_LOG2 (primitives sorted by alpha per shell)
         for (int si = lane; si < B.nshell; si += 32) {
-            const Shell sh = load_shell(B.shells + si);
+            const Shell sh = load_shell(B.mshells + si);
             const float ax = (float)B.atoms[4 * sh.atom], ay = (float)B.atoms[4 * sh.atom + 1],
                         az = (float)B.atoms[4 * sh.atom + 2];
             const float dx = fmaxf(0.f, fmaxf(v[0] - ax, ax - v[3]));
@@ -661,7 +661,7 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
             for (int si = ck.x; si < ck.y; ++si) {
                 const int nk = nkeep[si];
                 if (nk == 0) continue;
-                const unsigned w = (unsigned)(3 * nk + wcomp * ncanon(B.shells[si].L));
+                const unsigned w = (unsigned)(3 * nk + wcomp * ncanon(B.mshells[si].L));
                 unsigned v = (w << 16) | (unsigned)(si - ck.x);
                 int j = n++;
                 while (j > 0 && item[j - 1] < v) {
@@ -800,10 +800,10 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
     unsigned char* A_s = S.A_s + s * A_STAGE;
     if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status, S.wait_limit)) *S.abort_flag = 1;
     const int4 ck = B.mchunks[c];
-    Shell nx = load_shell(B.shells + ck.x);  // records are loaded one shell ahead
+    Shell nx = load_shell(B.mshells + ck.x);  // records are loaded one shell ahead
     for (int si = ck.x; si < ck.y; ++si) {
         const Shell sh = nx;
-        if (si + 1 < ck.y) nx = load_shell(B.shells + si + 1);
+        if (si + 1 < ck.y) nx = load_shell(B.mshells + si + 1);
         const int kb = nkeep[si];
         const int nk = kb & MAX_PRIM;
         if (nk == 0 || (kb >> KEEP_BITS) != grp) continue;
@@ -992,9 +992,11 @@ __device__ __forceinline__ void cusp_contract(const MolDesc& D, const CuspVals& 
 
 // Generation threads: the epilogue of one job.  Warp w reads TMEM lanes
 // 32 (w % 4) .. (its 32 points) and owns the outputs o (0 = rho, 1..3 = d/dx,
-// d/dy, d/dz) with o % E == w / 4 (E = generation warps / 4); the 8-MO groups are reduced in double-float
-// FP32 (exact products by FMA, two-sum accumulation, about 44 bits) and added to
-// the FP64 accumulators.
+// d/dy, d/dz) with o % E == w / 4 (E = generation warps / 4).  The MOs of the job
+// are reduced in double-float FP32 (exact products by FMA, two-sum accumulation,
+// about 44 bits), added once per job to the FP64 accumulators (GB300's FP64 pipe
+// retires two lanes per clock per SM: one FP64 sum per 8 MOs was a third of the
+// epilogue).
 template <int E, bool CUSP>
 __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nksteps, const CtaState& S,
                                              uint32_t& accseq, double (&acc)[4], const EpiPt& ep, CuspVals& cz,
@@ -1017,6 +1019,7 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
         const int nlead = nksteps < 4 ? nksteps : 4;  // leading accumulators written in this job
         int mo_end = D.nmo - pass * npad;
         mo_end = mo_end < npad ? (mo_end + 7) & ~7 : npad;
+        DF sacc[4];  // this job's double-float sums of the owned outputs
         for (int m0 = 0; m0 < mo_end; m0 += 8) {
             uint32_t q[5][8];
 #pragma unroll
@@ -1056,10 +1059,8 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
             }
             if (own[0]) {
                 if (!cusp) {
-                    DF sr;
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) sr.add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
-                    acc[0] += flt_to_dbl(sr.hi) + flt_to_dbl(sr.lo);
+                    for (int i = 0; i < 8; ++i) sacc[0].add(df_mul(__ldg(occf + m0 + i), v[i], v[i]));
                 } else {
                     const double* oc = D.occ + pass * npad + m0;
                     for (int i = 0; i < 8; ++i) {
@@ -1078,10 +1079,8 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
 #pragma unroll
                 for (int i = 0; i < 8; ++i) vd[i] = __uint_as_float(qd[0][i]);
                 if (!cusp) {
-                    DF sd;
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) sd.add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
-                    acc[o] += flt_to_dbl(sd.hi) + flt_to_dbl(sd.lo);
+                    for (int i = 0; i < 8; ++i) sacc[o].add(df_mul(__ldg(occ2f + m0 + i), v[i], vd[i]));
                 } else {
                     double cd[8];
                     if (cz.n >= 0)
@@ -1094,6 +1093,9 @@ __device__ __forceinline__ void gen_epilogue(const MolDesc& D, int pass, int nks
                 }
             }
         }
+#pragma unroll
+        for (int o = 0; o < 4; ++o)
+            if (own[o]) acc[o] += flt_to_dbl(sacc[o].hi) + flt_to_dbl(sacc[o].lo);
     }
     tc_fence_before();
     mbar_arrive(S.bar_acc_empty);
@@ -1806,6 +1808,7 @@ extern "C" int okg_mixed_plan_create_tiled(const okg_basis* b, int nmo, int n_ma
         return set_error(OKG_ERR_UNSUPPORTED, "okg_mixed_plan_create: a shell with more than 31 primitives");
     okg_mixed_plan* p = (okg_mixed_plan*)calloc(1, sizeof(okg_mixed_plan));
     if (!p) return set_error(OKG_ERR_ALLOC, "okg_mixed_plan_create: host allocation");
+    b->mixed_locked = 1;  // the coefficient tiles follow the basis's column order from now on
     p->basis = b;
     p->nmo = nmo;
     p->npass = (nmo + n_max - 1) / n_max;
@@ -2197,6 +2200,7 @@ extern "C" int okg_rho_mixed_noalloc(const okg_basis* b, const okg_grid* gr, int
         return set_error(OKG_ERR_UNSUPPORTED,
                          "okg_rho_mixed_noalloc: this basis and MO count need more than the 2 MiB of static "
                          "scratch; use okg_mixed_plan_create / okg_rho_mixed");
+    b->mixed_locked = 1;  // the column order read by the launch below stays as it is
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

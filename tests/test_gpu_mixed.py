@@ -183,6 +183,46 @@ def test_mixed_generation_layouts(mixed, layout):
         _check(mixed, r, gr, ro, go, "n=%d %s" % (n, layout))
 
 
+def test_mixed_column_order(mixed):
+    """okg_basis_set_mixed_order: the basis order, the exponent-class order the package
+    chooses and a reversed order all give the oracle's results; a non-permutation is
+    refused, and so is any reordering once a plan uses the basis."""
+    import ctypes
+    import torch
+    import okref
+    from orbkit_gb300 import synthetic, basis as bmod, _lib
+    from orbkit_gb300.core import _DeviceGrid
+    from orbkit_gb300.qcinfo import unpack
+    rng = numpy.random.default_rng(5)
+    w = synthetic.small()
+    qc = w["qc"]
+    geo, ao_spec, mo_spec = unpack(qc)
+    occ = numpy.array([m["occ_num"] for m in mo_spec], dtype=numpy.float64)
+    p = rng.uniform(-4, 4, (3, 3000))
+    ro, go = okref.rho_threads(qc, *p, drv=["x", "y", "z"], slice_length=1000, nthreads=2)
+    ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    for name in ("basis", "package", "reversed"):
+        b = bmod.DeviceBasis(geo, ao_spec)
+        if name != "package":
+            order = numpy.arange(b.nshell, dtype=numpy.int32)
+            if name == "reversed":
+                order = order[::-1].copy()
+            _lib.check(b._L.okg_basis_set_mixed_order(b.handle, ip(order)))
+        bad = numpy.zeros(b.nshell, dtype=numpy.int32)
+        with pytest.raises(_lib.OkgError):
+            _lib.check(b._L.okg_basis_set_mixed_order(b.handle, ip(bad)))
+        plan = mixed.MixedPlan(b, mo_spec.get_coeffs(), occ)
+        with pytest.raises(_lib.OkgError):
+            _lib.check(b._L.okg_basis_set_mixed_order(b.handle, ip(b.mixed_order)))
+        g = _DeviceGrid(p[0], p[1], p[2], True, b.device)
+        gd, keep = g.slice(0, g.npts)
+        r = torch.empty(g.npts, dtype=torch.float64, device=b.device)
+        gr = torch.empty((3, g.npts), dtype=torch.float64, device=b.device)
+        plan.rho(gd, r, gr, g.npts)
+        torch.cuda.synchronize()
+        _check(mixed, r.cpu().numpy(), gr.cpu().numpy(), ro, go, "order " + name)
+
+
 def test_mixed_through_drop_in_api(mixed):
     """core.rho_compute(..., precision='mixed') routes rho / grad rho to the tensor-core path."""
     from helpers import load_golden
