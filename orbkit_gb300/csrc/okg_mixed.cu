@@ -434,14 +434,42 @@ __device__ __forceinline__ Shell load_shell(const Shell* p)
     return s;
 }
 
+// Brick coordinates of a tile (32-bit division unless the grid is beyond 2^31 tiles).
+__device__ __forceinline__ void brick_of(const MolDesc& D, long long tile, int& bi, int& bj, int& bk)
+{
+    const long long nbyz = (long long)D.nby * D.nbz;
+    int rem;
+    if (tile < 0x7FFFFFFFll && nbyz < 0x7FFFFFFFll) {
+        bi = (int)tile / (int)nbyz;
+        rem = (int)tile - bi * (int)nbyz;
+    } else {
+        bi = (int)(tile / nbyz);
+        rem = (int)(tile - (long long)bi * nbyz);
+    }
+    bj = rem / D.nbz;
+    bk = rem - bj * D.nbz;
+}
+
+// The fields of a shell record that chunk generation reads (two of its three
+// 16-byte units).
+struct GenShell {
+    int atom, L, prim0, mcol;
+};
+
+__device__ __forceinline__ GenShell load_gen_shell(const Shell* p)
+{
+    const int4* q = reinterpret_cast<const int4*>(p);
+    const int4 a = __ldg(q), c = __ldg(q + 2);
+    return GenShell{a.x, a.y, a.w, c.z};
+}
+
 // Point of row r of a tile.
 __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int r, long long& p)
 {
     if (D.brick) {
-        const long long bi = tile / ((long long)D.nby * D.nbz);
-        const int rem = (int)(tile - bi * (long long)D.nby * D.nbz);
-        const int bj = rem / D.nbz, bk = rem - bj * D.nbz;
-        const int i = (int)bi * 4 + (r >> 5), j = bj * 4 + ((r >> 3) & 3), k = bk * 8 + (r & 7);
+        int bi, bj, bk;
+        brick_of(D, tile, bi, bj, bk);
+        const int i = bi * 4 + (r >> 5), j = bj * 4 + ((r >> 3) & 3), k = bk * 8 + (r & 7);
         if (i >= D.g.nx || j >= D.g.ny || k >= D.g.nz) {
             p = 0;
             return false;
@@ -455,6 +483,27 @@ __device__ __forceinline__ bool tile_point(const MolDesc& D, long long tile, int
         return false;
     }
     return true;
+}
+
+// The same with the point's coordinates; a brick reads its axis values directly (a
+// row outside the grid gets the nearest grid point's coordinates and p = 0).
+__device__ __forceinline__ bool tile_point_xyz(const MolDesc& D, long long tile, int r, long long& p, double& x,
+                                               double& y, double& z)
+{
+    if (D.brick) {
+        int bi, bj, bk;
+        brick_of(D, tile, bi, bj, bk);
+        const int i = bi * 4 + (r >> 5), j = bj * 4 + ((r >> 3) & 3), k = bk * 8 + (r & 7);
+        const bool valid = i < D.g.nx && j < D.g.ny && k < D.g.nz;
+        x = __ldg(D.g.x + (i < D.g.nx ? i : D.g.nx - 1));
+        y = __ldg(D.g.y + (j < D.g.ny ? j : D.g.ny - 1));
+        z = __ldg(D.g.z + (k < D.g.nz ? k : D.g.nz - 1));
+        p = valid ? ((long long)i * D.g.ny + j) * D.g.nz + k : 0;
+        return valid;
+    }
+    const bool valid = tile_point(D, tile, r, p);
+    grid_point(D.g, p, x, y, z);
+    return valid;
 }
 
 // K-steps (16 columns each) of a kept chunk that hold a kept column: the MMAs of a
@@ -557,21 +606,53 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
         }
         const MolDesc& D = S.mol[BATCH ? b : 0];
         const BasisDev& B = D.B;
-        // bounding box of the tile's valid points (four rows per lane)
+        // bounding box of the tile's valid points
         float v[6] = {3.0e38f, 3.0e38f, 3.0e38f, -3.0e38f, -3.0e38f, -3.0e38f};
+        if (D.brick) {
+            // a brick spans 4 x, 4 y and 8 z axis values (fewer at the grid's far
+            // faces): lanes 0-3, 4-7 and 8-15 take one each
+            const long long nbyz = (long long)D.nby * D.nbz;
+            const int bi = (int)(t / nbyz);
+            const int rem = (int)(t - (long long)bi * nbyz);
+            const int bj = rem / D.nbz, bk = rem - bj * D.nbz;
+            int axis = -1, idx = 0;
+            if (lane < 4) {
+                axis = 0;
+                idx = bi * 4 + lane;
+            } else if (lane < 8) {
+                axis = 1;
+                idx = bj * 4 + lane - 4;
+            } else if (lane < 16) {
+                axis = 2;
+                idx = bk * 8 + lane - 8;
+            }
+            const int n_ax = axis == 0 ? D.g.nx : axis == 1 ? D.g.ny : D.g.nz;
+            if (axis >= 0 && idx < n_ax) {
+                const double* ax = axis == 0 ? D.g.x : axis == 1 ? D.g.y : D.g.z;
+                const float c = dbl_to_flt_rn(__ldg(ax + idx));
 #pragma unroll
-        for (int i = 0; i < M / 32; ++i) {
-            long long pg;
-            if (tile_point(D, t, lane + 32 * i, pg)) {
-                double x, y, z;
-                grid_point(D.g, pg, x, y, z);
-                const float fx = dbl_to_flt_rn(x), fy = dbl_to_flt_rn(y), fz = dbl_to_flt_rn(z);
-                v[0] = fminf(v[0], fx);
-                v[1] = fminf(v[1], fy);
-                v[2] = fminf(v[2], fz);
-                v[3] = fmaxf(v[3], fx);
-                v[4] = fmaxf(v[4], fy);
-                v[5] = fmaxf(v[5], fz);
+                for (int a = 0; a < 3; ++a)
+                    if (a == axis) {
+                        v[a] = c;
+                        v[3 + a] = c;
+                    }
+            }
+        } else {
+            // runs of 128 points: four rows per lane
+#pragma unroll
+            for (int i = 0; i < M / 32; ++i) {
+                long long pg;
+                if (tile_point(D, t, lane + 32 * i, pg)) {
+                    double x, y, z;
+                    grid_point(D.g, pg, x, y, z);
+                    const float fx = dbl_to_flt_rn(x), fy = dbl_to_flt_rn(y), fz = dbl_to_flt_rn(z);
+                    v[0] = fminf(v[0], fx);
+                    v[1] = fminf(v[1], fy);
+                    v[2] = fminf(v[2], fz);
+                    v[3] = fmaxf(v[3], fx);
+                    v[4] = fmaxf(v[4], fy);
+                    v[5] = fmaxf(v[5], fz);
+                }
             }
         }
 #pragma unroll
@@ -628,8 +709,9 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
             const float dy = fmaxf(0.f, fmaxf(v[1] - ay, ay - v[4]));
             const float dz = fmaxf(0.f, fmaxf(v[2] - az, az - v[5]));
             const float d2 = dx * dx + dy * dy + dz * dz;
+            // (a count with independent loads: the kept primitives are a prefix)
             int nk = 0;
-            while (nk < sh.nprim && (float)B.prim_mx[sh.prim0 + nk].a2 * d2 <= SCREEN_LOG2) ++nk;
+            for (int k = 0; k < sh.nprim; ++k) nk += (float)B.prim_mx[sh.prim0 + k].a2 * d2 <= SCREEN_LOG2;
             if (CUSP) {
                 // a cusp atom of the tile keeps only its smooth primitives (alpha <= alpha_c, a
                 // prefix): the epilogue adds the steep ones in FP64 at every point of the tile
@@ -645,48 +727,36 @@ __device__ __forceinline__ void tile_role(const TileFeed& F, const CtaState& S, 
             if (nk > 0) atomicOr(km + sh.mchunk, ((1u << ncanon(sh.L)) - 1u) << sh.mcol);
         }
         __syncwarp();
-        // generation groups: per kept chunk, the kept shells in order of decreasing
-        // estimated work (kept primitives and components) each go to the group with the
-        // least work so far (longest-processing-time-first), so every group finishes the
-        // chunk at about the same time -- the stage's "full" barrier waits for all of
-        // them.  A group recomputes an atom's coordinates when its previous shell
-        // belonged to another atom.
+        // generation groups: per kept chunk (at most 32 shells, one per lane), the kept
+        // shells sorted by estimated work (kept primitives and components, bitonic sort
+        // across the warp) are dealt to the groups in snake order (0 1 .. NG-1 NG-1 .. 0
+        // 0 ..), so every group finishes the chunk at about the same time -- the stage's
+        // "full" barrier waits for all of them.  A group recomputes an atom's coordinates
+        // when its previous shell belonged to another atom.
         const int wcomp = D.want_grad ? 16 : 5;
-        for (int c = lane; c < B.nmchunk; c += 32) {
+        for (int c = 0; c < B.nmchunk; ++c) {
             if (km[c] == 0u) continue;
             const int4 ck = B.mchunks[c];
-            // (work << 16 | shell offset) of the kept shells, sorted descending
-            unsigned item[KC];
-            int n = 0;
-            for (int si = ck.x; si < ck.y; ++si) {
+            const int si = ck.x + lane;
+            unsigned key = 0u;  // work << 8 | shell offset; 0: no kept shell
+            if (si < ck.y) {
                 const int nk = nkeep[si];
-                if (nk == 0) continue;
-                const unsigned w = (unsigned)(3 * nk + wcomp * ncanon(B.mshells[si].L));
-                unsigned v = (w << 16) | (unsigned)(si - ck.x);
-                int j = n++;
-                while (j > 0 && item[j - 1] < v) {
-                    item[j] = item[j - 1];
-                    --j;
-                }
-                item[j] = v;
+                if (nk > 0) key = (unsigned)(3 * nk + wcomp * ncanon(B.mshells[si].L)) << 8 | (unsigned)lane;
             }
-            int load[NG];
 #pragma unroll
-            for (int g = 0; g < NG; ++g) load[g] = 0;
-            for (int i = 0; i < n; ++i) {
-                const int si = ck.x + (int)(item[i] & 0xFFFFu);
-                const int w = (int)(item[i] >> 16);
-                int gbest = 0, lbest = load[0];
+            for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
-                for (int g = 1; g < NG; ++g)
-                    if (load[g] < lbest) {
-                        lbest = load[g];
-                        gbest = g;
-                    }
-#pragma unroll
-                for (int g = 0; g < NG; ++g)
-                    if (g == gbest) load[g] += w;
-                nkeep[si] = (unsigned char)(nkeep[si] | (gbest << KEEP_BITS));
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    const unsigned other = __shfl_xor_sync(0xffffffffu, key, j);
+                    const bool take_max = ((lane & j) == 0) == ((lane & k) == 0);
+                    key = take_max ? max(key, other) : min(key, other);
+                }
+            }
+            if (key != 0u) {
+                const int turn = lane / NG, r = lane - turn * NG;
+                const int g = (turn & 1) ? NG - 1 - r : r;
+                const int sk = ck.x + (int)(key & 0xFFu);
+                nkeep[sk] = (unsigned char)(nkeep[sk] | (g << KEEP_BITS));
             }
         }
         __syncwarp();
@@ -712,19 +782,28 @@ __device__ __forceinline__ long long gen_open_tile(const CtaState& S, uint32_t o
     const long long tile = S.tile_slot[b];
     if (tile < 0) return -1;
     const MolDesc& D = S.mol[BATCH ? b : 0];
-    valid = tile_point(D, tile, 32 * (warp & 3) + lane, p);
+    // the epilogue row 32 (warp % 4) + lane is the generation row when P = 1
+    double ex, ey, ez;
+    valid = tile_point_xyz(D, tile, 32 * (warp & 3) + lane, p, ex, ey, ez);
     ep.ncusp = 0;
     if constexpr (CUSP) {
         const int* ca = S.cusp_atoms + b * (1 + NCA);
         ep.ncusp = valid ? ca[0] : 0;
         for (int i = 0; i < ep.ncusp; ++i) ep.atoms[i] = ca[1 + i];
-        if (ep.ncusp > 0) grid_point(D.g, p, ep.x, ep.y, ep.z);
+        ep.x = ex;
+        ep.y = ey;
+        ep.z = ez;
     }
+    if constexpr (P == 1) {
+        gp.x[0] = ex;
+        gp.y[0] = ey;
+        gp.z[0] = ez;
+    } else {
 #pragma unroll
-    for (int i = 0; i < P; ++i) {
-        long long pg;
-        tile_point(D, tile, P * (tid % (128 / P)) + i, pg);
-        grid_point(D.g, pg, gp.x[i], gp.y[i], gp.z[i]);
+        for (int i = 0; i < P; ++i) {
+            long long pg;
+            tile_point_xyz(D, tile, P * (tid % (128 / P)) + i, pg, gp.x[i], gp.y[i], gp.z[i]);
+        }
     }
     return tile;
 }
@@ -800,13 +879,23 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
     unsigned char* A_s = S.A_s + s * A_STAGE;
     if (u > 0 && !mbar_wait(S.bar_empty + 8 * s, (u - 1) & 1u, status, S.wait_limit)) *S.abort_flag = 1;
     const int4 ck = B.mchunks[c];
-    Shell nx = load_shell(B.mshells + ck.x);  // records are loaded one shell ahead
-    for (int si = ck.x; si < ck.y; ++si) {
-        const Shell sh = nx;
-        if (si + 1 < ck.y) nx = load_shell(B.mshells + si + 1);
-        const int kb = nkeep[si];
-        const int nk = kb & MAX_PRIM;
-        if (nk == 0 || (kb >> KEEP_BITS) != grp) continue;
+    // this group's kept shells of the chunk: the screening bytes are scanned, and the
+    // record of the next own shell is loaded one own shell ahead
+    auto next_own = [&](int t) {
+        for (; t < ck.y; ++t) {
+            const int kb = nkeep[t];
+            if ((kb & MAX_PRIM) != 0 && (kb >> KEEP_BITS) == grp) break;
+        }
+        return t;
+    };
+    int si = next_own(ck.x);
+    GenShell nx{0, 0, 0, 0};
+    if (si < ck.y) nx = load_gen_shell(B.mshells + si);
+    while (si < ck.y) {
+        const GenShell sh = nx;
+        const int nk = nkeep[si] & MAX_PRIM;
+        const int sn = next_own(si + 1);
+        if (sn < ck.y) nx = load_gen_shell(B.mshells + sn);
         if (sh.atom != ar.last_atom) {
             ar.last_atom = sh.atom;
             const double ax = B.atoms[4 * sh.atom], ay = B.atoms[4 * sh.atom + 1], az = B.atoms[4 * sh.atom + 2];
@@ -868,6 +957,7 @@ __device__ __forceinline__ void gen_chunk(const BasisDev& B, const unsigned char
                 *(__nv_bfloat162*)(base + 2 * A_TILE) = h2;
             });
         }
+        si = sn;
     }
     fence_proxy_async();
     mbar_arrive(S.bar_full + 8 * s);
