@@ -239,7 +239,10 @@ __device__ __forceinline__ float dbl_to_flt_trunc(double d)
 }
 
 // e^(-u ln 2) = 2^-u for an FP64 argument u >= 0 (u = alpha log2(e) r^2).
-// u = uh + r exactly with uh the float truncation of u; k = rint(uh),
+// u = uh + r exactly with uh the float truncation of u (its top 24 significant bits)
+// and r the remaining 29 mantissa bits, both taken from the bit pattern with integer
+// operations: r = (low 29 bits) 2^(e - 1075), converted toward zero to 24 bits (the
+// FP64 pipe is not used; below u = 2^-74 r is dropped).  k = rint(uh),
 // f = (uh - k) + r in FP32 (uh - k is exact), |f| <= 0.5 + 2^-23.  2^-f by the
 // degree-7 Taylor series of exp(y), y = -f ln 2 (|y| < 0.35, truncation error
 // < 6e-9 relative), scaled by 2^-k through the exponent field.
@@ -249,9 +252,9 @@ __device__ __forceinline__ float exp2_neg(double u)
     const int hi = __double2hiint(u);
     const unsigned lo = (unsigned)__double2loint(u);
     const double uh_d = __hiloint2double(hi, (int)(lo & 0xE0000000u));
-    const double rem = u - uh_d;  // exact
+    const int e = (hi >> 20) & 0x7FF;
     const float uh = dbl_to_flt_trunc(uh_d);
-    const float rf = dbl_to_flt_trunc(rem);
+    const float rf = e >= 949 ? __uint2float_rz(lo & 0x1FFFFFFFu) * __int_as_float((e - 948) << 23) : 0.0f;
     const float k = rintf(uh);
     const float f = (uh - k) + rf;
     const float y = -f * 0.693147180559945309f;
