@@ -95,6 +95,92 @@ def test_grid_operation_entry_points_validate_arguments(lib):
     assert lib.okg_mo_pair_flux(3, 4, 1, fake, fake, i64(8), fake, i64(8), i64(0), fake, i64(8), None) == 0
 
 
+def test_mixed_order_entry_point_rejects_null(lib):
+    """okg_basis_set_mixed_order checks its handle and order before any device work."""
+    lib.okg_basis_set_mixed_order.restype = ctypes.c_int
+    order = (ctypes.c_int * 2)(0, 1)
+    assert lib.okg_basis_set_mixed_order(None, order) == -1
+    assert lib.okg_basis_set_mixed_order(ctypes.c_void_p(16), None) == -1
+
+
+def _mixed_layout(order, ncols):
+    """Whole shells in `order` packed into 32-column chunks (the C builder's rule):
+    shell -> (chunk, first column)."""
+    col, chunk, pos = {}, 0, 0
+    for s in order:
+        if pos + ncols[s] > 32:
+            chunk, pos = chunk + 1, 0
+        col[s] = (chunk, pos)
+        pos += ncols[s]
+    return col, chunk + 1
+
+
+def test_mixed_order_is_exponent_classes_then_morton():
+    """The tensor-core column order: a permutation of the shells; factor-4 classes of the
+    smallest exponent ascending; inside a class, atoms along a Morton curve."""
+    from orbkit_gb300 import basis, synthetic
+    qc = synthetic.mid()["qc"]
+    f = basis.flatten(qc.ao_spec)
+    order = basis.mixed_order(qc.geo_spec, f)
+    assert sorted(order.tolist()) == list(range(len(f["nprim"])))
+    off = numpy.concatenate(([0], numpy.cumsum(f["nprim"])))
+    amin = numpy.array([f["prim"][off[s]:off[s + 1], 0].min() for s in range(len(f["nprim"]))])
+    cls = numpy.floor(numpy.log(amin) / numpy.log(4.0))[order]
+    assert numpy.all(numpy.diff(cls) >= 0)
+    # inside a class, the atoms' Morton codes do not decrease
+    geo = numpy.asarray(qc.geo_spec, dtype=float)
+    q = ((geo - geo.min(0)) / (geo.max(0) - geo.min(0)) * 1023).astype(numpy.int64)
+    code = numpy.zeros(len(geo), dtype=numpy.int64)
+    for b in range(10):
+        for d in range(3):
+            code |= ((q[:, d] >> b) & 1) << (3 * b + d)
+    at = numpy.asarray(f["atoms"])[order]
+    for c in numpy.unique(cls):
+        assert numpy.all(numpy.diff(code[at[cls == c]]) >= 0)
+    assert numpy.array_equal(order, basis.mixed_order(qc.geo_spec, f))
+
+
+def test_mixed_order_halves_issued_ksteps():
+    """Replay of the tensor-core kernel's screening on every 4x4x8 brick of the mid grid
+    (a primitive is kept while alpha log2(e) d^2 <= 64, d: distance from its atom to the
+    brick): the K-steps (16 columns) holding a kept column, per brick, in basis order and
+    in the package's order.  The GPU kernel counted 8.13 and 4.08."""
+    from orbkit_gb300 import basis, synthetic
+    w = synthetic.mid()
+    qc = w["qc"]
+    gx, gy, gz = w["grid"]
+    f = basis.flatten(qc.ao_spec)
+    geo = numpy.asarray(qc.geo_spec, dtype=float)
+    ncols = [(L + 1) * (L + 2) // 2 for L in
+             (numpy.asarray(f["lxlylz"])[numpy.concatenate(([0], numpy.cumsum(f["ncart"])))[:-1]].sum(1))]
+    off = numpy.concatenate(([0], numpy.cumsum(f["nprim"])))
+    amin = numpy.array([f["prim"][off[s]:off[s + 1], 0].min() for s in range(len(ncols))])
+
+    def box(ax, n):
+        return numpy.array([(ax[i], ax[min(i + n - 1, len(ax) - 1)]) for i in range(0, len(ax), n)])
+
+    bx, by, bz = box(gx, 4), box(gy, 4), box(gz, 8)
+    dist = lambda b, a: numpy.maximum(0.0, numpy.maximum(b[:, 0] - a, a - b[:, 1]))
+    kept = numpy.zeros((len(bx) * len(by) * len(bz), len(ncols)), dtype=bool)
+    for s in range(len(ncols)):
+        a = geo[f["atoms"][s]]
+        d2 = (dist(bx, a[0])[:, None, None] ** 2 + dist(by, a[1])[None, :, None] ** 2 +
+              dist(bz, a[2])[None, None, :] ** 2).ravel()
+        kept[:, s] = amin[s] * 1.4426950408889634 * d2 <= 64.0
+
+    def ksteps(order):
+        col, nchunk = _mixed_layout(order, ncols)
+        M = numpy.zeros((len(ncols), 2 * nchunk), dtype=numpy.int32)
+        for s, (c, p) in col.items():
+            for k in range(p, p + ncols[s]):
+                M[s, 2 * c + k // 16] = 1
+        return ((kept.astype(numpy.int32) @ M) > 0).sum(1).mean()
+
+    before = ksteps(list(range(len(ncols))))
+    after = ksteps(basis.mixed_order(geo, f).tolist())
+    assert abs(before - 8.13) < 0.02 and abs(after - 4.08) < 0.02, (before, after)
+
+
 def _overlap_plan(lib, lxlylz, ncart, nprim=None, atoms=None, natom=1):
     ip = lambda a: (ctypes.c_int * len(a))(*a)
     nshell = len(ncart)
