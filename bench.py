@@ -409,6 +409,8 @@ def run_profile(args):
         return _profile_large()
     if args.workload == "ao":
         return _profile_ao()
+    if args.workload == "batch":
+        return _profile_batch()
     import torch
     from orbkit_gb300 import _lib, mixed, synthetic
     from orbkit_gb300.core import _DeviceGrid
@@ -464,6 +466,33 @@ def _profile_large():
     torch.cuda.synchronize()
     ev.check()
     print("profile run done: large, %d points mixed, %d FP64" % (n, n64))
+
+
+def _profile_batch():
+    """A 12-molecule batch (10-30 atoms each, atom-centred point sets, 6.1 M points) on
+    the persistent batch kernel, three launches with the FP64 cusp region in the launch
+    and three from the tensor cores alone (schedule fixed: 384 x 1, 64 MO columns)."""
+    import torch
+    from orbkit_gb300 import synthetic
+    from orbkit_gb300.batch import BatchEvaluator
+    torch.cuda.set_device(0)
+    d = synthetic.batch(nmol=12, min_atoms=10, max_atoms=30)
+    mols = [(m["qc"], m["points"]) for m in d["molecules"]]
+    npts = sum(pp.shape[1] for _, pp in mols)
+    sch = {"n_max": 64, "grab": 1, "order": "largest_first", "layout": (384, 1)}
+    for radius in (None, 0.0):
+        ev = BatchEvaluator(mols, tune=False, cusp_radius=radius, schedule=sch)
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            ev.run()
+            e1.record()
+            torch.cuda.synchronize()
+            print("batch %s: %d points, %.3f ms" % ("FP64 cusp region" if radius is None else "tensor cores alone",
+                                                   npts, e0.elapsed_time(e1)))
+        ev.check()
+    print("profile run done: batch")
 
 
 def _profile_ao():
